@@ -1,0 +1,184 @@
+/*
+ * torque_gb300.h -- C ABI of the GB300-native block-sparse contraction library.
+ *
+ * The drop-in boundary for Torque's block-sparse GPU path
+ * (torque::gpu::BlockSparseTensor<T>, src/gpu/block_sparse.cuh).  The C++
+ * header include/torque_gb300/block_sparse.hpp rebuilds the reference class on
+ * top of these entry points; other languages bind them directly (ctypes, cgo,
+ * JNI: see INTEGRATION.md).
+ *
+ * Conventions kept from the reference:
+ *   - column-major: leg 0 is fastest (src/util/space.h:11-24);
+ *   - metadata matrices are rank x n_blocks with one column per block, passed
+ *     as flat arrays where block b, leg l is element [b*rank + l] (the memory
+ *     layout of an arma::umat);
+ *   - boxes are inclusive [begin, end] per leg; they may overlap, and query sums
+ *     every block containing the index (block_sparse.cuh:506-552);
+ *   - block data are back to back; block_offsets = exclusive scan of the block
+ *     element counts (src/util/space.h:77-88).
+ * Changes from the reference:
+ *   - every call returns a tq_status instead of exit()ing the process
+ *     (src/gpu/util/lib_helper.cuh:39-77); tq_last_error_string() explains it;
+ *   - work is ordered on the caller's stream; only calls that must hand a
+ *     number to the host (query, to_number, metadata reads, output sizing in
+ *     contract) synchronise that stream;
+ *   - no cuBLAS/cuTT handle: contract takes none.
+ */
+#ifndef TORQUE_GB300_H
+#define TORQUE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *tq_stream; /* a cudaStream_t; NULL = legacy default */
+
+typedef enum {
+  TQ_OK = 0,
+  TQ_ERR_INVALID = 1,     /* API misuse: the reference throws Error here */
+  TQ_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+  TQ_ERR_OOM = 3,         /* device allocation failed (or was refused by the hook) */
+  TQ_ERR_RANGE = 4,       /* index outside the tensor */
+  TQ_ERR_UNSUPPORTED = 5, /* valid input outside what this build implements */
+  TQ_ERR_TIMEOUT = 6      /* a bounded device wait gave up */
+} tq_status;
+
+typedef enum { TQ_F32 = 0, TQ_F64 = 1 } tq_dtype;
+
+typedef enum { TQ_MEM_HOST = 0, TQ_MEM_DEVICE = 1 } tq_memkind;
+
+/* Arithmetic of the block GEMMs. */
+typedef enum {
+  TQ_PREC_NATIVE = 0, /* plain arithmetic in the tensor's type (the drop-in) */
+  TQ_PREC_OZAKI = 1,  /* FP64-level: exact integer slices on the bf16 tensor cores */
+  TQ_PREC_BF16X3 = 2  /* FP32-level: three-way bf16 split products */
+} tq_precision;
+
+/* Block list of a contraction result. */
+typedef enum {
+  TQ_LAYOUT_REFERENCE = 0, /* one output block per matched block pair, in the
+                              reference's order (block_sparse.cuh:626-674) */
+  TQ_LAYOUT_REDUCED = 1    /* one block per distinct output box, partials of the
+                              pairs that land in it summed in FP64 */
+} tq_layout;
+
+typedef struct {
+  int32_t precision; /* tq_precision */
+  int32_t layout;    /* tq_layout */
+  int32_t slices;    /* Ozaki slice count (0 = default); ignored otherwise */
+  int32_t reserved;
+} tq_contract_opts;
+
+typedef struct tq_bs tq_bs; /* opaque block-sparse tensor */
+
+/* ---- construction ---------------------------------------------------- */
+
+/* BlockSparseTensor(const arma::uvec & dimension)
+ * (src/gpu/block_sparse.cuh:180-187): no blocks; a rank-0 tensor holds one
+ * zero. */
+tq_status tq_bs_create_empty(tq_dtype dtype, int32_t rank, const int64_t *dimension,
+                             tq_bs **out);
+
+/* BlockSparseTensor(const T*, const umat& begin, const umat& end,
+ *                   const uvec& dim, cudaMemcpyKind) (block_sparse.cuh:189-236),
+ * and with explicit index tables (block_sparse.cuh:238-281).  index_tables may
+ * be NULL (column-major strides of each block, the reference's default). */
+tq_status tq_bs_create(tq_dtype dtype, int32_t rank, const int64_t *dimension,
+                       int64_t n_blocks, const int64_t *begin_points,
+                       const int64_t *end_points, const int64_t *index_tables,
+                       const void *data, tq_memkind kind, tq_stream stream,
+                       tq_bs **out);
+
+/* Copy constructor (block_sparse.cuh:306-327): deep device copy. */
+tq_status tq_bs_clone(const tq_bs *t, tq_stream stream, tq_bs **out);
+
+/* Destructor (block_sparse.cuh:361-364). */
+tq_status tq_bs_destroy(tq_bs *t);
+
+/* append_block / append_blocks (block_sparse.cuh:376-446).  The buffer grows
+ * geometrically instead of being reallocated per call. */
+tq_status tq_bs_append_blocks(tq_bs *t, int64_t n_blocks, const int64_t *begin_points,
+                              const int64_t *end_points, const int64_t *index_tables,
+                              const void *data, tq_memkind kind, tq_stream stream);
+
+/* ---- element access ---------------------------------------------------- */
+
+/* query (block_sparse.cuh:506-552): sum over every block holding the index. */
+tq_status tq_bs_query(const tq_bs *t, const int64_t *indices, void *value);
+
+/* modify (block_sparse.cuh:451-502): set in the first block holding the index,
+ * zero it in the others, or append a one-element block if none holds it and
+ * the value is nonzero. */
+tq_status tq_bs_modify(tq_bs *t, const int64_t *indices, const void *value);
+
+/* to_number (block_sparse.cuh:367-374): the value of a rank-0 tensor. */
+tq_status tq_bs_to_number(const tq_bs *t, void *value);
+
+/* ---- metadata ---------------------------------------------------------- */
+
+tq_status tq_bs_shape(const tq_bs *t, tq_dtype *dtype, int32_t *rank, int64_t *n_blocks,
+                      int64_t *n_elem);
+/* The public members dimension, begin_points, end_points, index_tables,
+ * block_offsets (block_sparse.cuh:147-178).  Any pointer may be NULL. */
+tq_status tq_bs_metadata(const tq_bs *t, int64_t *dimension, int64_t *begin_points,
+                         int64_t *end_points, int64_t *index_tables,
+                         int64_t *block_offsets);
+/* The device buffer (the reference's protected T* data). */
+tq_status tq_bs_device_data(const tq_bs *t, void **ptr);
+/* Copy all block data to dst (host or device), ordered on stream. */
+tq_status tq_bs_copy_data(const tq_bs *t, void *dst, tq_memkind kind, tq_stream stream);
+
+/* ---- operations -------------------------------------------------------- */
+
+/* contract (block_sparse.cuh:558-1026): contract legs a_legs[k] of A with
+ * b_legs[k] of B (the two columns of the reference's n x 2 contracting_indices).
+ * The result's legs are A's free legs then B's free legs, each in order.
+ * opts may be NULL (native precision, reference layout). */
+tq_status tq_bs_contract(const tq_bs *A, const tq_bs *B, int32_t n_legs,
+                         const int64_t *a_legs, const int64_t *b_legs,
+                         const tq_contract_opts *opts, tq_stream stream, tq_bs **out);
+
+/* hard_transpose (block_sparse.cuh:1031-1122): permute the legs of every block;
+ * new leg l is old leg perm[l]. */
+tq_status tq_bs_hard_transpose(const tq_bs *t, const int64_t *perm, tq_stream stream,
+                               tq_bs **out);
+
+/* slice (block_sparse.cuh:1124-1176): split every block into prod(divisor)
+ * boxes without moving data, as the reference does. */
+tq_status tq_bs_slice(const tq_bs *t, const int64_t *divisor, tq_stream stream,
+                      tq_bs **out);
+
+/* ---- plans: the symbolic and numeric stages of contract, separately ------- */
+
+typedef struct tq_plan tq_plan;
+
+/* Runs the index kernels (pair matching, output boxes and offsets), allocates
+ * the result and returns it with its metadata filled and its data not yet
+ * computed.  Synchronises the stream once to size the result. */
+tq_status tq_plan_create(const tq_bs *A, const tq_bs *B, int32_t n_legs,
+                         const int64_t *a_legs, const int64_t *b_legs,
+                         const tq_contract_opts *opts, tq_stream stream,
+                         tq_plan **plan, tq_bs **out);
+/* Numeric stage: computes the result's data.  No host synchronisation, no
+ * allocation: safe to capture in a CUDA graph.  A and B must be alive. */
+tq_status tq_plan_execute(tq_plan *plan, tq_stream stream);
+/* Useful flops of the plan: sum over matched block pairs of 2*m*n*k. */
+tq_status tq_plan_flops(const tq_plan *plan, double *flops, int64_t *n_pairs);
+tq_status tq_plan_destroy(tq_plan *plan);
+
+/* ---- errors and hooks -------------------------------------------------- */
+
+/* Message of the last failing call on this thread. */
+const char *tq_last_error_string(void);
+
+/* Test hook: the next `after` device allocations succeed, then every one is
+ * refused with TQ_ERR_OOM until reset with after < 0. */
+void tq_debug_fail_alloc_after(int64_t after);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

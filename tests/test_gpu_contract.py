@@ -1,0 +1,161 @@
+"""Parity of the CUDA contraction path with the oracle (through the C ABI via
+the Python mirror).  Integer work (pair list, boxes, offsets) is bit-exact;
+FP64 values agree within 1e-12 of max|C| (the reference's tolerance claim),
+FP32 within 1e-5."""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from torque_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 1e-5
+
+
+def to_gpu(tq, dim, begin, end, data, tables=None, dtype=np.float64):
+    return tq.BlockSparseTensor(dim, np.asarray(data, dtype), np.asarray(begin).T,
+                                np.asarray(end).T,
+                                None if tables is None else np.asarray(tables).T, dtype=dtype)
+
+
+def host(dim, begin, end, data, tables=None):
+    return orc.HostBS(np.asarray(dim), begin, end, data, strides=tables)
+
+
+@pytest.fixture(scope="module")
+def small():
+    return workloads.small_u1()
+
+
+def check_reference_layout(tq, A, B, hA, hB, pairs, dtype=np.float64, tol=TOL64):
+    C = A.contract(B, pairs)
+    ob, oe, off, want = orc.contract(hA, hB, pairs, mode=0)
+    dim, b, e, t, o = C.metadata()
+    assert np.array_equal(b.T, ob) and np.array_equal(e.T, oe)
+    assert np.array_equal(o, off)
+    dims = oe - ob + 1
+    st = np.ones_like(dims)
+    st[:, 1:] = np.cumprod(dims[:, :-1], axis=1)
+    assert np.array_equal(t.T, st)
+    got = C.data().astype(np.float64)
+    assert got.shape == want.shape
+    assert np.max(np.abs(got - want)) <= tol * max(np.max(np.abs(want)), 1e-300)
+    return C
+
+
+def test_small_u1_reference_layout(tq, small):
+    c = small
+    A = to_gpu(tq, c.A.dimension, c.A.begin, c.A.end, c.a_data)
+    B = to_gpu(tq, c.B.dimension, c.B.begin, c.B.end, c.b_data)
+    hA = host(c.A.dimension, c.A.begin, c.A.end, c.a_data)
+    hB = host(c.B.dimension, c.B.begin, c.B.end, c.b_data)
+    C = check_reference_layout(tq, A, B, hA, hB, c.pairs)
+    assert C.n_blocks == 325
+
+
+def test_small_u1_reduced_layout(tq, small):
+    c = small
+    A = to_gpu(tq, c.A.dimension, c.A.begin, c.A.end, c.a_data)
+    B = to_gpu(tq, c.B.dimension, c.B.begin, c.B.end, c.b_data)
+    hA = host(c.A.dimension, c.A.begin, c.A.end, c.a_data)
+    hB = host(c.B.dimension, c.B.begin, c.B.end, c.b_data)
+    C = A.contract(B, c.pairs, layout="reduced")
+    assert C.n_blocks == 85
+    dim, b, e, t, o = C.metadata()
+    ob, oe, off, data = orc.contract(hA, hB, c.pairs, mode=0)
+    boxes = np.unique(np.concatenate([ob, oe], 1), axis=0)
+    order = np.lexsort(boxes[:, :4].T)  # leg 0 least significant: column-major sector order
+    assert np.array_equal(b.T, boxes[order, :4]) and np.array_equal(e.T, boxes[order, 4:])
+    got = orc.densify(host(dim, b.T, e.T, C.data(), t.T))
+    want = orc.dense_contract(orc.densify(hA), orc.densify(hB), c.pairs)
+    assert np.max(np.abs(got - want)) <= TOL64 * np.max(np.abs(want))
+
+
+def test_small_u1_float32(tq, small):
+    c = small
+    A = to_gpu(tq, c.A.dimension, c.A.begin, c.A.end, c.a_data, dtype=np.float32)
+    B = to_gpu(tq, c.B.dimension, c.B.begin, c.B.end, c.b_data, dtype=np.float32)
+    a32 = c.a_data.astype(np.float32).astype(np.float64)
+    b32 = c.b_data.astype(np.float32).astype(np.float64)
+    hA = host(c.A.dimension, c.A.begin, c.A.end, a32)
+    hB = host(c.B.dimension, c.B.begin, c.B.end, b32)
+    check_reference_layout(tq, A, B, hA, hB, c.pairs, np.float32, TOL32)
+
+
+def test_non_adjacent_free_legs(tq, small):
+    """Contract the middle legs: A's free legs (0, 3) are not stride-contiguous,
+    so the operand view keeps two row legs (general addressing path)."""
+    c = small
+    A = to_gpu(tq, c.A.dimension, c.A.begin, c.A.end, c.a_data)
+    B = to_gpu(tq, c.B.dimension, c.B.begin, c.B.end, c.b_data)
+    hA = host(c.A.dimension, c.A.begin, c.A.end, c.a_data)
+    hB = host(c.B.dimension, c.B.begin, c.B.end, c.b_data)
+    for pairs in ([[1, 0], [2, 1]], [[3, 2], [0, 3]], [[1, 3]]):
+        check_reference_layout(tq, A, B, hA, hB, np.array(pairs))
+
+
+@pytest.mark.parametrize("perm", [[1, 0, 2, 3], [3, 2, 1, 0], [0, 1, 3, 2], [2, 0, 3, 1]])
+def test_hard_transpose_bit_exact(tq, small, perm):
+    c = small
+    A = to_gpu(tq, c.A.dimension, c.A.begin, c.A.end, c.a_data)
+    hA = host(c.A.dimension, c.A.begin, c.A.end, c.a_data)
+    T = A.hard_transpose(perm)
+    want = orc.hard_transpose(hA, perm)
+    dim, b, e, t, o = T.metadata()
+    assert np.array_equal(dim, want.dimension)
+    assert np.array_equal(b.T, want.begin) and np.array_equal(e.T, want.end)
+    assert np.array_equal(T.data(), want.data)
+
+
+def test_partial_overlaps_and_custom_strides(tq):
+    rng = np.random.default_rng(5)
+    dimA = [6, 7, 5]
+    bA, eA = [[0, 0, 0], [2, 3, 1], [1, 0, 2]], [[3, 4, 2], [5, 6, 4], [4, 2, 4]]
+    nA = 4 * 5 * 3 + 4 * 4 * 4 + 4 * 3 * 3
+    dA = rng.standard_normal(nA)
+    dimB = [7, 4]
+    bB, eB = [[1, 0], [4, 1], [0, 2]], [[5, 2], [6, 3], [2, 3]]
+    # B's blocks stored row-major: index tables (d1, 1) instead of (1, d0)
+    tB = [[3, 1], [3, 1], [2, 1]]
+    dB = rng.standard_normal(5 * 3 + 3 * 3 + 3 * 2)
+    A = to_gpu(tq, dimA, bA, eA, dA)
+    B = to_gpu(tq, dimB, bB, eB, dB, tB)
+    hA = host(dimA, bA, eA, dA)
+    hB = host(dimB, bB, eB, dB, tB)
+    for pairs in ([[1, 0]], [[0, 1]], [[2, 1]]):
+        check_reference_layout(tq, A, B, hA, hB, np.array(pairs))
+    # full contraction to a scalar over two legs: A[0:2, 1:3, 2] x B as a 2-leg tensor
+    s = A.contract(A, [[0, 0], [1, 1], [2, 2]]).to_number()
+    assert abs(s - orc.contract(hA, hA, [[0, 0], [1, 1], [2, 2]])) <= 1e-12 * abs(s)
+
+
+def test_empty_and_unmatched(tq):
+    A = tq.BlockSparseTensor([4, 4])
+    B = tq.BlockSparseTensor([4, 4])
+    C = A.contract(B, [[1, 0]])
+    assert C.n_blocks == 0 and C.query([1, 1]) == 0
+    A.append_block(np.ones(4), [0, 0], [1, 1])
+    B.append_block(np.ones(4), [2, 2], [3, 3])
+    C = A.contract(B, [[1, 0]])
+    assert C.n_blocks == 0
+    assert A.contract(B, [[1, 0], [0, 1]]).to_number() == 0
+    assert A.contract(B, [[1, 0]], layout="reduced").n_blocks == 0
+
+
+def test_allocation_failure_is_reported(tq, small):
+    c = small
+    A = to_gpu(tq, c.A.dimension, c.A.begin, c.A.end, c.a_data)
+    B = to_gpu(tq, c.B.dimension, c.B.begin, c.B.end, c.b_data)
+    lib = tq.load()
+    for after in (0, 1, 3, 6):
+        lib.tq_debug_fail_alloc_after(after)
+        try:
+            with pytest.raises(tq.TorqueError) as ei:
+                A.contract(B, c.pairs)
+            assert ei.value.status == 3
+        finally:
+            lib.tq_debug_fail_alloc_after(-1)
+    C = A.contract(B, c.pairs)  # the library still works afterwards
+    assert C.n_blocks == 325

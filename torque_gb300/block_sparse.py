@@ -1,0 +1,296 @@
+"""Python mirror of torque::gpu::BlockSparseTensor<T> over the C ABI.
+
+Same names, argument meaning and error behaviour as the reference class
+(src/gpu/block_sparse.cuh:143-1181): metadata matrices are rank x n_blocks
+(column = block, the arma::umat convention), legs are column-major with leg 0
+fastest, API misuse raises TorqueError (the reference's ``Error``).  Every
+operation runs on the GPU through libtorque_gb300.so; nothing here computes.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import TQ_F32, TQ_F64, TQ_MEM_DEVICE, TQ_MEM_HOST, ContractOpts, check, load
+
+_DT = {np.dtype(np.float64): TQ_F64, np.dtype(np.float32): TQ_F32}
+_NP = {TQ_F64: np.float64, TQ_F32: np.float32}
+
+
+def _i64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int64))
+
+
+def _p64(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)) if a.size else None
+
+
+def _stream(stream) -> Optional[int]:
+    if stream is None:
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return stream.cuda_stream
+    return int(stream)
+
+
+def _blocks(points, rank: int) -> np.ndarray:
+    """rank x n_blocks (arma::umat layout) -> flat [b*rank + l]."""
+    a = np.asarray(points, dtype=np.int64)
+    if a.ndim == 1:
+        a = a.reshape(rank, -1) if rank else a.reshape(0, -1)
+    if a.shape[0] != rank:
+        raise _lib.TorqueError(_lib.TQ_ERR_INVALID, "Rank does not match")
+    return np.ascontiguousarray(a.T)
+
+
+class BlockSparseTensor:
+    """A list of dense boxes (blocks) of a rank-r tensor, data on the GPU."""
+
+    def __init__(self, dimension=None, source_data=None, begin_points=None, end_points=None,
+                 index_tables=None, dtype=np.float64, stream=None, _handle=None):
+        load()
+        self._h = ctypes.c_void_p()
+        if _handle is not None:
+            self._h = _handle
+            return
+        dim = _i64(dimension if dimension is not None else [])
+        rank = dim.size
+        dt = _DT[np.dtype(dtype)]
+        if source_data is None:
+            # BlockSparseTensor(const arma::uvec & dimension)
+            check(load().tq_bs_create_empty(dt, rank, _p64(dim), ctypes.byref(self._h)))
+            return
+        data, kind = self._data_arg(source_data, dtype)
+        b = _blocks(begin_points, rank)
+        e = _blocks(end_points, rank)
+        t = None if index_tables is None else _blocks(index_tables, rank)
+        self._keep = data
+        check(load().tq_bs_create(dt, rank, _p64(dim), b.shape[0] if rank else 0, _p64(b), _p64(e),
+                                  None if t is None else _p64(t), self._ptr(data), kind,
+                                  _stream(stream), ctypes.byref(self._h)))
+        self._keep = None
+
+    # ------------------------------------------------------------ helpers
+    @staticmethod
+    def _data_arg(src, dtype):
+        if hasattr(src, "data_ptr"):  # a torch tensor on the device
+            return src, TQ_MEM_DEVICE
+        return np.ascontiguousarray(np.asarray(src, dtype=dtype)), TQ_MEM_HOST
+
+    @staticmethod
+    def _ptr(data):
+        if hasattr(data, "data_ptr"):
+            return ctypes.c_void_p(data.data_ptr())
+        return data.ctypes.data_as(ctypes.c_void_p)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                load().tq_bs_destroy(h)
+            except Exception:  # interpreter shutdown
+                pass
+            self._h = ctypes.c_void_p()
+
+    def _shape(self):
+        dt = ctypes.c_int32()
+        rank = ctypes.c_int32()
+        nb = ctypes.c_int64()
+        ne = ctypes.c_int64()
+        check(load().tq_bs_shape(self._h, ctypes.byref(dt), ctypes.byref(rank), ctypes.byref(nb),
+                                 ctypes.byref(ne)))
+        return dt.value, rank.value, nb.value, ne.value
+
+    # ------------------------------------------------------------ metadata
+    @property
+    def dtype(self):
+        return np.dtype(_NP[self._shape()[0]])
+
+    @property
+    def rank(self) -> int:
+        return self._shape()[1]
+
+    @property
+    def n_blocks(self) -> int:
+        return self._shape()[2]
+
+    @property
+    def n_elem(self) -> int:
+        return self._shape()[3]
+
+    def metadata(self):
+        """(dimension, begin_points, end_points, index_tables, block_offsets); the
+        point matrices are rank x n_blocks."""
+        _, r, nb, _ = self._shape()
+        dim = np.zeros(r, np.int64)
+        b = np.zeros((nb, r), np.int64)
+        e = np.zeros((nb, r), np.int64)
+        t = np.zeros((nb, r), np.int64)
+        off = np.zeros(nb, np.int64)
+        check(load().tq_bs_metadata(self._h, _p64(dim), _p64(b), _p64(e), _p64(t), _p64(off)))
+        return dim, b.T.copy(), e.T.copy(), t.T.copy(), off
+
+    @property
+    def dimension(self):
+        return self.metadata()[0]
+
+    @property
+    def begin_points(self):
+        return self.metadata()[1]
+
+    @property
+    def end_points(self):
+        return self.metadata()[2]
+
+    @property
+    def index_tables(self):
+        return self.metadata()[3]
+
+    @property
+    def block_offsets(self):
+        return self.metadata()[4]
+
+    @property
+    def blocks_dimension(self):
+        _, b, e, _, _ = self.metadata()
+        return e - b + 1
+
+    @property
+    def block_n_elem(self):
+        return np.prod(self.blocks_dimension, axis=0)
+
+    def data(self) -> np.ndarray:
+        """Host copy of the block data (all blocks back to back)."""
+        dt, r, _, ne = self._shape()
+        out = np.zeros(1 if r == 0 else ne, _NP[dt])
+        if out.size:
+            check(load().tq_bs_copy_data(self._h, out.ctypes.data_as(ctypes.c_void_p), TQ_MEM_HOST,
+                                         None))
+        return out
+
+    def device_ptr(self) -> int:
+        p = ctypes.c_void_p()
+        check(load().tq_bs_device_data(self._h, ctypes.byref(p)))
+        return p.value or 0
+
+    # ------------------------------------------------------------ element access
+    def to_number(self):
+        v = np.zeros(1, self.dtype)
+        check(load().tq_bs_to_number(self._h, v.ctypes.data_as(ctypes.c_void_p)))
+        return v[0]
+
+    def query(self, indices: Sequence[int]):
+        idx = _i64(indices)
+        if idx.size != self.rank:
+            raise _lib.TorqueError(_lib.TQ_ERR_INVALID, "Rank does not match")
+        v = np.zeros(1, self.dtype)
+        check(load().tq_bs_query(self._h, _p64(idx), v.ctypes.data_as(ctypes.c_void_p)))
+        return v[0]
+
+    def modify(self, indices: Sequence[int], number):
+        idx = _i64(indices)
+        if idx.size != self.rank:
+            raise _lib.TorqueError(_lib.TQ_ERR_INVALID, "Rank does not match")
+        v = np.asarray([number], self.dtype)
+        check(load().tq_bs_modify(self._h, _p64(idx), v.ctypes.data_as(ctypes.c_void_p)))
+
+    def append_block(self, source_data, begin_point, end_point, index_table=None, stream=None):
+        self.append_blocks(source_data, np.asarray(begin_point).reshape(-1, 1),
+                           np.asarray(end_point).reshape(-1, 1),
+                           None if index_table is None else np.asarray(index_table).reshape(-1, 1),
+                           stream)
+
+    def append_blocks(self, source_data, begin_points, end_points, index_tables=None, stream=None):
+        r = self.rank
+        b = _blocks(begin_points, r)
+        e = _blocks(end_points, r)
+        t = None if index_tables is None else _blocks(index_tables, r)
+        data, kind = self._data_arg(source_data, self.dtype)
+        check(load().tq_bs_append_blocks(self._h, b.shape[0], _p64(b), _p64(e),
+                                         None if t is None else _p64(t), self._ptr(data), kind,
+                                         _stream(stream)))
+
+    # ------------------------------------------------------------ operations
+    def contract(self, tensor: "BlockSparseTensor", contracting_indices, precision="native",
+                 layout="reference", slices=0, stream=None) -> "BlockSparseTensor":
+        """Contract legs contracting_indices[k][0] of self with [k][1] of tensor
+        (an n x 2 matrix, as in the reference)."""
+        ci = np.asarray(contracting_indices, dtype=np.int64).reshape(-1, 2)
+        al, bl = _i64(ci[:, 0]), _i64(ci[:, 1])
+        opts = ContractOpts(_lib.PRECISIONS[precision], _lib.LAYOUTS[layout], slices, 0)
+        h = ctypes.c_void_p()
+        check(load().tq_bs_contract(self._h, tensor._h, ci.shape[0], _p64(al), _p64(bl),
+                                    ctypes.byref(opts), _stream(stream), ctypes.byref(h)))
+        return BlockSparseTensor(_handle=h)
+
+    def hard_transpose(self, permutation, stream=None) -> "BlockSparseTensor":
+        perm = _i64(permutation)
+        if perm.size != self.rank:
+            raise _lib.TorqueError(_lib.TQ_ERR_INVALID,
+                                   "The number of permutation does not match the rank of tensor")
+        h = ctypes.c_void_p()
+        check(load().tq_bs_hard_transpose(self._h, _p64(perm), _stream(stream), ctypes.byref(h)))
+        return BlockSparseTensor(_handle=h)
+
+    def slice(self, divisor, stream=None) -> "BlockSparseTensor":
+        d = _i64(divisor)
+        h = ctypes.c_void_p()
+        check(load().tq_bs_slice(self._h, _p64(d), _stream(stream), ctypes.byref(h)))
+        return BlockSparseTensor(_handle=h)
+
+    def clone(self, stream=None) -> "BlockSparseTensor":
+        h = ctypes.c_void_p()
+        check(load().tq_bs_clone(self._h, _stream(stream), ctypes.byref(h)))
+        return BlockSparseTensor(_handle=h)
+
+
+class ContractionPlan:
+    """The symbolic stage of a contraction, kept for repeated numeric runs
+    (tq_plan_create / tq_plan_execute)."""
+
+    def __init__(self, A: BlockSparseTensor, B: BlockSparseTensor, contracting_indices,
+                 precision="native", layout="reference", slices=0, stream=None):
+        ci = np.asarray(contracting_indices, dtype=np.int64).reshape(-1, 2)
+        al, bl = _i64(ci[:, 0]), _i64(ci[:, 1])
+        opts = ContractOpts(_lib.PRECISIONS[precision], _lib.LAYOUTS[layout], slices, 0)
+        self._p = ctypes.c_void_p()
+        h = ctypes.c_void_p()
+        self.A, self.B = A, B  # keep the operands alive
+        check(load().tq_plan_create(A._h, B._h, ci.shape[0], _p64(al), _p64(bl),
+                                    ctypes.byref(opts), _stream(stream), ctypes.byref(self._p),
+                                    ctypes.byref(h)))
+        self.result = BlockSparseTensor(_handle=h)
+
+    def execute(self, stream=None):
+        check(load().tq_plan_execute(self._p, _stream(stream)))
+        return self.result
+
+    @property
+    def flops(self) -> float:
+        f = ctypes.c_double()
+        n = ctypes.c_int64()
+        check(load().tq_plan_flops(self._p, ctypes.byref(f), ctypes.byref(n)))
+        return f.value
+
+    @property
+    def n_pairs(self) -> int:
+        f = ctypes.c_double()
+        n = ctypes.c_int64()
+        check(load().tq_plan_flops(self._p, ctypes.byref(f), ctypes.byref(n)))
+        return n.value
+
+    def __del__(self):
+        p = getattr(self, "_p", None)
+        if p is not None and p.value:
+            try:
+                load().tq_plan_destroy(p)
+            except Exception:
+                pass
+            self._p = ctypes.c_void_p()

@@ -1,0 +1,437 @@
+// contract: the symbolic stage (index kernels, output boxes and offsets) and
+// the numeric stage (grouped GEMM) of torque::gpu::BlockSparseTensor::contract
+// (src/gpu/block_sparse.cuh:558-1026).
+//
+// Symbolic stage, all on the device:
+//   1. match: per A block the B blocks whose contracted intervals overlap
+//      (counts -> exclusive scan -> ordered emit): the pair list in the
+//      reference's order, A ascending then B ascending (block_sparse.cuh:626-652);
+//   2. output boxes: A free legs ++ B free legs of each pair
+//      (src/tensor/block_sparse.cpp:66-119); offsets = exclusive scan of the
+//      element counts (block_sparse.cuh:658-674);
+//   3. reduced layout only: pairs keyed by their output box (interval ids of the
+//      free legs), stably radix-sorted, segmented: one output block per key.
+// One host synchronisation reads the sizes and allocates the result.
+#include <algorithm>
+#include <cstring>
+
+#include "gemm.cuh"
+#include "index.cuh"
+#include "plan.cuh"
+
+namespace tq {
+
+// ---------------------------------------------------------------- kernels
+__global__ void pair_stats_kernel(DevBS A, DevBS B, LegSpec L, const int32_t *pa,
+                                  const int32_t *pb, int64_t n_pairs, int64_t *mnk,
+                                  int64_t *chunks) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_pairs) return;
+  const int64_t i = pa[p], j = pb[p];
+  int64_t m = 1, n = 1, k = 1;
+  for (int q = 0; q < L.nfa; q++)
+    m *= A.end[i * A.rank + L.fa[q]] - A.begin[i * A.rank + L.fa[q]] + 1;
+  for (int q = 0; q < L.nfb; q++)
+    n *= B.end[j * B.rank + L.fb[q]] - B.begin[j * B.rank + L.fb[q]] + 1;
+  int64_t cb[TQ_MAXR], ce[TQ_MAXR];
+  contraction_range(A, B, L, i, j, cb, ce);
+  for (int c = 0; c < L.nc; c++) k *= ce[c] - cb[c] + 1;
+  mnk[p] = m * n * k;
+  if (chunks) chunks[p] = (k + DOT_CHUNK - 1) / DOT_CHUNK;
+}
+
+// Output block o: box of its first pair; column-major strides; element and
+// tile counts.
+__global__ void out_meta_kernel(DevBS A, DevBS B, LegSpec L, const int32_t *pa,
+                                const int32_t *pb, const int64_t *seg, const int64_t *perm,
+                                int64_t n_out, int32_t rc, int64_t *c_begin, int64_t *c_end,
+                                int64_t *c_strides, int64_t *n_elem, int64_t *tiles) {
+  const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= n_out) return;
+  const int64_t p0 = perm ? perm[seg[o]] : seg[o];
+  const int64_t i = pa[p0], j = pb[p0];
+  int64_t stride = 1, m = 1, n = 1;
+  for (int q = 0; q < rc; q++) {
+    int64_t b, e;
+    if (q < L.nfa) {
+      b = A.begin[i * A.rank + L.fa[q]];
+      e = A.end[i * A.rank + L.fa[q]];
+      m *= e - b + 1;
+    } else {
+      b = B.begin[j * B.rank + L.fb[q - L.nfa]];
+      e = B.end[j * B.rank + L.fb[q - L.nfa]];
+      n *= e - b + 1;
+    }
+    c_begin[o * rc + q] = b;
+    c_end[o * rc + q] = e;
+    c_strides[o * rc + q] = stride;
+    stride *= e - b + 1;
+  }
+  n_elem[o] = stride;
+  tiles[o] = ((m + NT_TM - 1) / NT_TM) * ((n + NT_TN - 1) / NT_TN);
+}
+
+__global__ void iota_kernel(int64_t *x, int64_t n) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < n) x[p] = p;
+}
+
+// --- interval ids of one leg (for the reduced layout) ------------------------
+// For every block: its interval [b, e] on `leg`.  The leg is "laminar" when any
+// two intervals are equal or disjoint; the id of an interval is then the rank
+// of its begin among all begins.
+__global__ void mark_intervals_kernel(DevBS T, int32_t leg, int64_t *is_begin,
+                                      unsigned long long *emin, unsigned long long *emax) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= T.nb) return;
+  const int64_t x = T.begin[b * T.rank + leg];
+  const unsigned long long e = (unsigned long long)T.end[b * T.rank + leg];
+  is_begin[x] = 1;
+  atomicMin(&emin[x], e);
+  atomicMax(&emax[x], e);
+}
+
+__global__ void check_intervals_kernel(const int64_t *is_begin, const int64_t *ids, int64_t dim,
+                                       const unsigned long long *emin,
+                                       const unsigned long long *emax, int64_t *begin_of_id,
+                                       int32_t *bad) {
+  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= dim || !is_begin[x]) return;
+  if (emin[x] != emax[x]) atomicOr(bad, 1);
+  begin_of_id[ids[x]] = x;
+}
+
+__global__ void check_disjoint_kernel(const int64_t *begin_of_id, int64_t n_ids,
+                                      const unsigned long long *emax, int32_t *bad) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t + 1 >= n_ids) return;
+  if ((int64_t)emax[begin_of_id[t]] >= begin_of_id[t + 1]) atomicOr(bad, 1);
+}
+
+__global__ void block_key_kernel(DevBS T, int32_t leg, const int64_t *ids, int64_t radix,
+                                 int64_t *key) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= T.nb) return;
+  key[b] += ids[T.begin[b * T.rank + leg]] * radix;
+}
+
+__global__ void pair_key_kernel(const int32_t *pa, const int32_t *pb, int64_t n,
+                                const int64_t *ka, const int64_t *kb, int64_t KA, int64_t *key) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < n) key[p] = ka[pa[p]] + KA * kb[pb[p]];
+}
+
+__global__ void seg_flag_kernel(const int64_t *key, int64_t n, int64_t *flag) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) flag[s] = (s == 0 || key[s] != key[s - 1]) ? 1 : 0;
+}
+
+__global__ void seg_start_kernel(const int64_t *flag, const int64_t *sid, int64_t n,
+                                 int64_t n_out, int64_t *seg) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n && flag[s]) seg[sid[s]] = s;
+  if (s == 0) seg[n_out] = n;
+}
+
+static inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+// Interval-id keys of every block of T over `legs` (mixed radix, first leg
+// fastest).  *K receives the key range; returns UNSUPPORTED if a leg is not
+// laminar or the key range overflows.
+static tq_status box_keys(const tq_bs *T, int32_t nlegs, const int32_t *legs, int64_t *key,
+                          int64_t *K, cudaStream_t s) {
+  TQ_CUDA(cudaMemsetAsync(key, 0, sizeof(int64_t) * std::max<int64_t>(T->nb, 1), s));
+  int64_t radix = 1;
+  DevArray<int32_t> bad;
+  TQ_CHECK(bad.alloc(1, s));
+  for (int32_t q = 0; q < nlegs; q++) {
+    const int32_t leg = legs[q];
+    const int64_t dim = T->dimension[leg];
+    DevArray<int64_t> is_begin, ids, begin_of_id, total;
+    DevArray<unsigned long long> emin, emax;
+    TQ_CHECK(is_begin.alloc(dim, s));
+    TQ_CHECK(ids.alloc(dim, s));
+    TQ_CHECK(begin_of_id.alloc(dim, s));
+    TQ_CHECK(total.alloc(1, s));
+    TQ_CHECK(emin.alloc(dim, s));
+    TQ_CHECK(emax.alloc(dim, s));
+    TQ_CUDA(cudaMemsetAsync(is_begin.p, 0, dim * 8, s));
+    TQ_CUDA(cudaMemsetAsync(emin.p, 0xff, dim * 8, s));
+    TQ_CUDA(cudaMemsetAsync(emax.p, 0, dim * 8, s));
+    TQ_CUDA(cudaMemsetAsync(bad.p, 0, 4, s));
+    const DevBS v = T->view();
+    mark_intervals_kernel<<<nblk(T->nb), 256, 0, s>>>(v, leg, is_begin.p, emin.p, emax.p);
+    TQ_CHECK(scan_exclusive(is_begin.p, ids.p, dim, total.p, s));
+    check_intervals_kernel<<<nblk(dim), 256, 0, s>>>(is_begin.p, ids.p, dim, emin.p, emax.p,
+                                                     begin_of_id.p, bad.p);
+    int64_t n_ids = 0;
+    int32_t h_bad = 0;
+    TQ_CUDA(cudaMemcpyAsync(&n_ids, total.p, 8, cudaMemcpyDeviceToHost, s));
+    TQ_CUDA(cudaStreamSynchronize(s));
+    check_disjoint_kernel<<<nblk(std::max<int64_t>(n_ids, 1)), 256, 0, s>>>(begin_of_id.p, n_ids,
+                                                                           emax.p, bad.p);
+    block_key_kernel<<<nblk(T->nb), 256, 0, s>>>(v, leg, ids.p, radix, key);
+    TQ_CUDA(cudaGetLastError());
+    TQ_CUDA(cudaMemcpyAsync(&h_bad, bad.p, 4, cudaMemcpyDeviceToHost, s));
+    TQ_CUDA(cudaStreamSynchronize(s));
+    if (h_bad)
+      return fail(TQ_ERR_UNSUPPORTED,
+                  "reduced layout needs the free legs' intervals to be equal or disjoint "
+                  "(sector boxes); use the reference layout");
+    if (n_ids > 0 && radix > (int64_t(1) << 62) / n_ids)
+      return fail(TQ_ERR_UNSUPPORTED, "output box key range exceeds 2^62");
+    radix *= std::max<int64_t>(n_ids, 1);
+  }
+  *K = radix;
+  return TQ_OK;
+}
+
+static int bits_for(int64_t K) {
+  int b = 0;
+  while (b < 63 && (int64_t(1) << b) < K) b++;
+  return b;
+}
+
+tq_status validate_legs(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,
+                        const int64_t *b_legs, LegSpec &L) {
+  if (!A || !B) return fail(TQ_ERR_INVALID, "tensor is NULL");
+  if (A->dtype != B->dtype) return fail(TQ_ERR_INVALID, "tensors have different dtypes");
+  if (n_legs < 0 || n_legs > TQ_MAXR) return fail(TQ_ERR_INVALID, "bad number of contracted legs");
+  if (n_legs && (!a_legs || !b_legs)) return fail(TQ_ERR_INVALID, "leg lists are NULL");
+  std::memset(&L, 0, sizeof(L));
+  L.nc = n_legs;
+  L.rank_a = A->rank;
+  L.rank_b = B->rank;
+  bool used_a[TQ_MAXR] = {false}, used_b[TQ_MAXR] = {false};
+  for (int32_t k = 0; k < n_legs; k++) {
+    if (a_legs[k] < 0 || a_legs[k] >= A->rank || b_legs[k] < 0 || b_legs[k] >= B->rank)
+      return fail(TQ_ERR_INVALID, "contracted leg index out of range");
+    if (used_a[a_legs[k]] || used_b[b_legs[k]])
+      return fail(TQ_ERR_INVALID, "a leg is contracted twice");
+    used_a[a_legs[k]] = used_b[b_legs[k]] = true;
+    if (A->dimension[a_legs[k]] != B->dimension[b_legs[k]])
+      return fail(TQ_ERR_INVALID, "The dimensions from two tensors to be contracted do not match");
+    L.al[k] = (int32_t)a_legs[k];
+    L.bl[k] = (int32_t)b_legs[k];
+  }
+  for (int32_t l = 0; l < A->rank; l++)
+    if (!used_a[l]) L.fa[L.nfa++] = l;
+  for (int32_t l = 0; l < B->rank; l++)
+    if (!used_b[l]) L.fb[L.nfb++] = l;
+  return TQ_OK;
+}
+
+tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,
+                     const int64_t *b_legs, const tq_contract_opts *opts, cudaStream_t s,
+                     tq_plan **plan_out, tq_bs **out) {
+  LegSpec L;
+  TQ_CHECK(validate_legs(A, B, n_legs, a_legs, b_legs, L));
+  tq_contract_opts o = {TQ_PREC_NATIVE, TQ_LAYOUT_REFERENCE, 0, 0};
+  if (opts) o = *opts;
+  if (o.precision != TQ_PREC_NATIVE && o.precision != TQ_PREC_OZAKI &&
+      o.precision != TQ_PREC_BF16X3)
+    return fail(TQ_ERR_INVALID, "unknown precision");
+  if (o.precision != TQ_PREC_NATIVE && A->dtype != TQ_F64)
+    return fail(TQ_ERR_UNSUPPORTED, "tensor-core forms take float64 tensors");
+  if (o.layout != TQ_LAYOUT_REFERENCE && o.layout != TQ_LAYOUT_REDUCED)
+    return fail(TQ_ERR_INVALID, "unknown layout");
+  TQ_CHECK(sync_device_meta(const_cast<tq_bs *>(A), s));
+  TQ_CHECK(sync_device_meta(const_cast<tq_bs *>(B), s));
+
+  std::unique_ptr<tq_plan> P(new tq_plan());
+  P->A = A;
+  P->B = B;
+  P->L = L;
+  P->opts = o;
+  const int32_t rc = L.nfa + L.nfb;
+  std::vector<int64_t> new_dim;
+  for (int q = 0; q < L.nfa; q++) new_dim.push_back(A->dimension[L.fa[q]]);
+  for (int q = 0; q < L.nfb; q++) new_dim.push_back(B->dimension[L.fb[q]]);
+  if (rc > TQ_MAXR) return fail(TQ_ERR_UNSUPPORTED, "result rank above 12");
+  const DevBS Av = A->view(), Bv = B->view();
+
+  // 1. pairs
+  DevArray<int64_t> counts, row_off, tot;
+  TQ_CHECK(counts.alloc(std::max<int64_t>(A->nb, 1), s));
+  TQ_CHECK(row_off.alloc(std::max<int64_t>(A->nb, 1), s));
+  TQ_CHECK(tot.alloc(4, s));
+  TQ_CHECK(match_pairs(Av, Bv, L, counts.p, s));
+  TQ_CHECK(scan_exclusive(counts.p, row_off.p, A->nb, tot.p, s));
+  int64_t n_pairs = 0;
+  TQ_CUDA(cudaMemcpyAsync(&n_pairs, tot.p, 8, cudaMemcpyDeviceToHost, s));
+  TQ_CUDA(cudaStreamSynchronize(s));
+  if (n_pairs > 0x7fffffffLL) return fail(TQ_ERR_UNSUPPORTED, "more than 2^31 block pairs");
+  P->n_pairs = n_pairs;
+  TQ_CHECK(P->pa.alloc(std::max<int64_t>(n_pairs, 1), s));
+  TQ_CHECK(P->pb.alloc(std::max<int64_t>(n_pairs, 1), s));
+  TQ_CHECK(emit_pairs(Av, Bv, L, row_off.p, P->pa.p, P->pb.p, s));
+
+  // per-pair work (m*n*k) for the flop count; dot chunks for rank-0 results
+  DevArray<int64_t> mnk, mnk_off;
+  TQ_CHECK(mnk.alloc(std::max<int64_t>(n_pairs, 1), s));
+  TQ_CHECK(mnk_off.alloc(std::max<int64_t>(n_pairs, 1), s));
+  DevArray<int64_t> chunks;
+  if (rc == 0) {
+    TQ_CHECK(chunks.alloc(std::max<int64_t>(n_pairs, 1), s));
+    TQ_CHECK(P->chunk_start.alloc(std::max<int64_t>(n_pairs, 1), s));
+  }
+  if (n_pairs) {
+    pair_stats_kernel<<<nblk(n_pairs), 256, 0, s>>>(Av, Bv, L, P->pa.p, P->pb.p, n_pairs, mnk.p,
+                                                     rc == 0 ? chunks.p : nullptr);
+    TQ_CUDA(cudaGetLastError());
+  }
+  TQ_CHECK(scan_exclusive(mnk.p, mnk_off.p, n_pairs, tot.p + 1, s));
+
+  tq_bs *C = new_tensor(A->dtype, rc, new_dim.data());
+  std::unique_ptr<tq_bs, tq_status (*)(tq_bs *)> Cguard(C, tq_bs_destroy);
+
+  if (rc == 0) {
+    // rank-0 result: one scalar, sum over all pairs
+    TQ_CHECK(scan_exclusive(chunks.p, P->chunk_start.p, n_pairs, tot.p + 2, s));
+    int64_t h[3] = {0, 0, 0};
+    TQ_CUDA(cudaMemcpyAsync(h, tot.p, 24, cudaMemcpyDeviceToHost, s));
+    TQ_CUDA(cudaStreamSynchronize(s));
+    P->flops = 2.0 * (double)h[1];
+    P->n_chunks = h[2];
+    TQ_CHECK(P->partials.alloc(std::max<int64_t>(P->n_chunks, 1), s));
+    TQ_CHECK(alloc_data(C, 1, s));
+    C->nb = 0;
+    C->host_valid = true;
+    C->dev_valid = true;
+    P->n_out = 0;
+  } else {
+    int64_t n_out = n_pairs;
+    if (o.layout == TQ_LAYOUT_REDUCED && n_pairs) {
+      // 3. group pairs by output box
+      DevArray<int64_t> ka, kb, key, flag, sid;
+      int64_t KA = 1, KB = 1;
+      TQ_CHECK(ka.alloc(std::max<int64_t>(A->nb, 1), s));
+      TQ_CHECK(kb.alloc(std::max<int64_t>(B->nb, 1), s));
+      TQ_CHECK(box_keys(A, L.nfa, L.fa, ka.p, &KA, s));
+      TQ_CHECK(box_keys(B, L.nfb, L.fb, kb.p, &KB, s));
+      if (KB > 0 && KA > (int64_t(1) << 62) / KB)
+        return fail(TQ_ERR_UNSUPPORTED, "output box key range exceeds 2^62");
+      TQ_CHECK(key.alloc(n_pairs, s));
+      TQ_CHECK(P->perm.alloc(n_pairs, s));
+      pair_key_kernel<<<nblk(n_pairs), 256, 0, s>>>(P->pa.p, P->pb.p, n_pairs, ka.p, kb.p, KA,
+                                                    key.p);
+      iota_kernel<<<nblk(n_pairs), 256, 0, s>>>(P->perm.p, n_pairs);
+      TQ_CUDA(cudaGetLastError());
+      TQ_CHECK(radix_sort_pairs(key.p, P->perm.p, n_pairs, bits_for(KA * KB), s));
+      TQ_CHECK(flag.alloc(n_pairs, s));
+      TQ_CHECK(sid.alloc(n_pairs, s));
+      seg_flag_kernel<<<nblk(n_pairs), 256, 0, s>>>(key.p, n_pairs, flag.p);
+      TQ_CHECK(scan_exclusive(flag.p, sid.p, n_pairs, tot.p + 3, s));
+      TQ_CUDA(cudaMemcpyAsync(&n_out, tot.p + 3, 8, cudaMemcpyDeviceToHost, s));
+      TQ_CUDA(cudaStreamSynchronize(s));
+      TQ_CHECK(P->seg.alloc(n_out + 1, s));
+      seg_start_kernel<<<nblk(n_pairs), 256, 0, s>>>(flag.p, sid.p, n_pairs, n_out, P->seg.p);
+      TQ_CUDA(cudaGetLastError());
+    } else {
+      TQ_CHECK(P->seg.alloc(n_pairs + 1, s));
+      iota_kernel<<<nblk(n_pairs + 1), 256, 0, s>>>(P->seg.p, n_pairs + 1);
+      TQ_CUDA(cudaGetLastError());
+    }
+    P->n_out = n_out;
+    // 2. output metadata: boxes, strides, element counts, offsets; tiles
+    C->nb = n_out;
+    TQ_CHECK(C->d_meta.alloc(3 * (size_t)n_out * rc + n_out, s));
+    DevArray<int64_t> n_elem, tiles;
+    TQ_CHECK(n_elem.alloc(std::max<int64_t>(n_out, 1), s));
+    TQ_CHECK(tiles.alloc(std::max<int64_t>(n_out, 1), s));
+    TQ_CHECK(P->tile_start.alloc(n_out + 1, s));
+    if (n_out) {
+      int64_t *cb = C->d_meta.p, *ce = cb + n_out * rc, *cs = ce + n_out * rc;
+      out_meta_kernel<<<nblk(n_out), 256, 0, s>>>(Av, Bv, L, P->pa.p, P->pb.p, P->seg.p,
+                                                  P->perm.p, n_out, rc, cb, ce, cs, n_elem.p,
+                                                  tiles.p);
+      TQ_CUDA(cudaGetLastError());
+    }
+    int64_t *c_off = C->d_meta.p + 3 * n_out * rc;
+    TQ_CHECK(scan_exclusive(n_elem.p, c_off, n_out, tot.p + 2, s));
+    TQ_CHECK(scan_exclusive(tiles.p, P->tile_start.p, n_out, tot.p + 3, s));
+    int64_t h[4] = {0, 0, 0, 0};
+    TQ_CUDA(cudaMemcpyAsync(h, tot.p, 32, cudaMemcpyDeviceToHost, s));
+    TQ_CUDA(cudaStreamSynchronize(s));
+    P->flops = 2.0 * (double)h[1];
+    P->n_tiles = h[3];
+    TQ_CHECK(alloc_data(C, h[2], s));
+    C->host_valid = false;
+    C->dev_valid = true;
+  }
+  P->C = C;
+  Cguard.release();
+  *out = C;
+  *plan_out = P.release();
+  return TQ_OK;
+}
+
+tq_status plan_run(tq_plan *P, cudaStream_t s) {
+  GemmJob job;
+  job.A = P->A->view();
+  job.B = P->B->view();
+  job.L = P->L;
+  job.pa = P->pa.p;
+  job.pb = P->pb.p;
+  job.seg = P->seg.p;
+  job.perm = P->perm.p;
+  job.tile_start = P->tile_start.p;
+  job.c_off = P->C->d_meta.p ? P->C->d_meta.p + 3 * P->n_out * P->C->rank : nullptr;
+  job.C = P->C->data;
+  job.n_out = P->n_out;
+  if (P->C->rank == 0)
+    return launch_dot_native(job, P->n_pairs, P->chunk_start.p, P->n_chunks, P->partials.p,
+                             P->A->dtype, s);
+  if (P->n_tiles == 0) return TQ_OK;
+  return launch_gemm_native(job, P->n_tiles, P->A->dtype, s);
+}
+
+}  // namespace tq
+
+using namespace tq;
+
+extern "C" {
+
+tq_status tq_plan_create(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,
+                         const int64_t *b_legs, const tq_contract_opts *opts, tq_stream stream,
+                         tq_plan **plan, tq_bs **out) {
+  if (!plan || !out) return fail(TQ_ERR_INVALID, "NULL output argument");
+  return plan_build(A, B, n_legs, a_legs, b_legs, opts, (cudaStream_t)stream, plan, out);
+}
+
+tq_status tq_plan_execute(tq_plan *plan, tq_stream stream) {
+  if (!plan) return fail(TQ_ERR_INVALID, "plan is NULL");
+  return plan_run(plan, (cudaStream_t)stream);
+}
+
+tq_status tq_plan_flops(const tq_plan *plan, double *flops, int64_t *n_pairs) {
+  if (!plan) return fail(TQ_ERR_INVALID, "plan is NULL");
+  if (flops) *flops = plan->flops;
+  if (n_pairs) *n_pairs = plan->n_pairs;
+  return TQ_OK;
+}
+
+tq_status tq_plan_destroy(tq_plan *plan) {
+  delete plan;
+  return TQ_OK;
+}
+
+tq_status tq_bs_contract(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,
+                         const int64_t *b_legs, const tq_contract_opts *opts, tq_stream stream,
+                         tq_bs **out) {
+  if (!out) return fail(TQ_ERR_INVALID, "out is NULL");
+  tq_plan *P = nullptr;
+  tq_bs *C = nullptr;
+  TQ_CHECK(plan_build(A, B, n_legs, a_legs, b_legs, opts, (cudaStream_t)stream, &P, &C));
+  tq_status st = plan_run(P, (cudaStream_t)stream);
+  // the plan's scratch is released stream-ordered after the kernels that use it
+  tq_plan_destroy(P);
+  if (st != TQ_OK) {
+    tq_bs_destroy(C);
+    return st;
+  }
+  *out = C;
+  return TQ_OK;
+}
+
+}  // extern "C"
