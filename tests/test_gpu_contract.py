@@ -124,8 +124,16 @@ def test_partial_overlaps_and_custom_strides(tq):
     B = to_gpu(tq, dimB, bB, eB, dB, tB)
     hA = host(dimA, bA, eA, dA)
     hB = host(dimB, bB, eB, dB, tB)
-    for pairs in ([[1, 0]], [[0, 1]], [[2, 1]]):
-        check_reference_layout(tq, A, B, hA, hB, np.array(pairs))
+    check_reference_layout(tq, A, B, hA, hB, np.array([[1, 0]]))
+    # a second operand over A's legs 0 and 2, stored with permuted strides
+    dimD = [6, 5]
+    bD, eD = [[0, 0], [3, 2], [2, 1]], [[4, 3], [5, 4], [3, 4]]
+    tD = [[4, 1], [3, 1], [4, 1]]
+    dD = rng.standard_normal(5 * 4 + 3 * 3 + 2 * 4)
+    D = to_gpu(tq, dimD, bD, eD, dD, tD)
+    hD = host(dimD, bD, eD, dD, tD)
+    for pairs in ([[0, 0]], [[2, 1]], [[0, 0], [2, 1]], [[2, 1], [0, 0]]):
+        check_reference_layout(tq, A, D, hA, hD, np.array(pairs))
     # full contraction to a scalar over two legs: A[0:2, 1:3, 2] x B as a 2-leg tensor
     s = A.contract(A, [[0, 0], [1, 1], [2, 2]]).to_number()
     assert abs(s - orc.contract(hA, hA, [[0, 0], [1, 1], [2, 2]])) <= 1e-12 * abs(s)

@@ -17,6 +17,7 @@
 
 #include "gemm.cuh"
 #include "index.cuh"
+#include "ozaki.cuh"
 #include "plan.cuh"
 
 namespace tq {
@@ -192,6 +193,192 @@ static int bits_for(int64_t K) {
   return b;
 }
 
+// ---------------------------------------------------------------- tensor-core plan
+// The sliced forms take sector-aligned pairs: every matched pair covers the same
+// full interval of both blocks on each contracted leg (true for charge-sector
+// tensors), so each block is sliced once and shared by all its pairs.
+__global__ void tc_align_kernel(DevBS A, DevBS B, LegSpec L, const int32_t *pa, const int32_t *pb,
+                                int64_t n, int32_t *bad) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int64_t i = pa[p], j = pb[p];
+  for (int k = 0; k < L.nc; k++)
+    if (A.begin[i * A.rank + L.al[k]] != B.begin[j * B.rank + L.bl[k]] ||
+        A.end[i * A.rank + L.al[k]] != B.end[j * B.rank + L.bl[k]])
+      atomicOr(bad, 1);
+}
+
+__global__ void tc_block_stats_kernel(OzSide S, int32_t rt_rows, int32_t slices, int64_t *mkey,
+                                      int64_t *rows, int64_t *tiles, int64_t *units) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= S.T.nb) return;
+  int64_t m = 1, k = 1;
+  for (int q = 0; q < S.nfree; q++)
+    m *= S.T.end[b * S.T.rank + S.free_legs[q]] - S.T.begin[b * S.T.rank + S.free_legs[q]] + 1;
+  for (int q = 0; q < S.ncon; q++)
+    k *= S.T.end[b * S.T.rank + S.con[q]] - S.T.begin[b * S.T.rank + S.con[q]] + 1;
+  rows[b] = m;
+  tiles[b] = (m + rt_rows - 1) / rt_rows;
+  units[b] = ((k + 15) / 16) * slices * ((m + 7) / 8);
+  mkey[S.key[b]] = m;
+}
+
+__global__ void tc_out_kernel(DevBS A, DevBS B, LegSpec L, const int32_t *pa, const int32_t *pb,
+                              const int64_t *seg, const int64_t *perm, int64_t n_out,
+                              int32_t *nk_pair, int64_t *tiles, int64_t *ksum) {
+  const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= n_out) return;
+  int64_t tot = 0;
+  for (int64_t sidx = seg[o]; sidx < seg[o + 1]; sidx++) {
+    const int64_t p = perm ? perm[sidx] : sidx;
+    const int64_t i = pa[p];
+    int64_t k = 1;
+    for (int q = 0; q < L.nc; q++)
+      k *= A.end[i * A.rank + L.al[q]] - A.begin[i * A.rank + L.al[q]] + 1;
+    nk_pair[p] = (int32_t)((k + 15) / 16);
+    tot += (k + 15) / 16;
+  }
+  ksum[o] = tot;
+  const int64_t p0 = perm ? perm[seg[o]] : seg[o];
+  int64_t m = 1, n = 1;
+  for (int q = 0; q < L.nfa; q++)
+    m *= A.end[pa[p0] * A.rank + L.fa[q]] - A.begin[pa[p0] * A.rank + L.fa[q]] + 1;
+  for (int q = 0; q < L.nfb; q++)
+    n *= B.end[pb[p0] * B.rank + L.fb[q]] - B.begin[pb[p0] * B.rank + L.fb[q]] + 1;
+  tiles[o] = ((m + OZ_M - 1) / OZ_M) * ((n + OZ_N - 1) / OZ_N);
+}
+
+static OzSide make_side(const tq_bs *T, int32_t nfree, const int32_t *fl, int32_t ncon,
+                        const int32_t *con, const int64_t *key, const int64_t *row_off,
+                        const int64_t *row_start, const int64_t *tile_start,
+                        const int64_t *unit_off) {
+  OzSide S;
+  std::memset(&S, 0, sizeof(S));
+  S.T = T->view();
+  S.nfree = nfree;
+  S.ncon = ncon;
+  for (int q = 0; q < nfree; q++) S.free_legs[q] = fl[q];
+  for (int q = 0; q < ncon; q++) S.con[q] = con[q];
+  S.key = key;
+  S.row_off = row_off;
+  S.row_start = row_start;
+  S.tile_start = tile_start;
+  S.unit_off = unit_off;
+  return S;
+}
+
+static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
+  const LegSpec &L = P->L;
+  const tq_bs *A = P->A, *B = P->B;
+  int32_t sl = P->opts.slices;
+  if (sl == 0) sl = P->opts.precision == TQ_PREC_OZAKI ? 5 : 3;
+  if (sl < 1 || sl > OZ_MAXS) return fail(TQ_ERR_INVALID, "slice count outside 1..7");
+  P->slices = sl;
+  if (KA > (1 << 26) || KB > (1 << 26))
+    return fail(TQ_ERR_UNSUPPORTED, "too many distinct free boxes for the sliced forms");
+  const int64_t np = P->n_pairs, no = P->n_out;
+  DevArray<int32_t> bad;
+  TQ_CHECK(bad.alloc(1, s));
+  TQ_CUDA(cudaMemsetAsync(bad.p, 0, 4, s));
+  tc_align_kernel<<<nblk(np), 256, 0, s>>>(A->view(), B->view(), L, P->pa.p, P->pb.p, np, bad.p);
+  TQ_CUDA(cudaGetLastError());
+  // per-block geometry of both sides
+  DevArray<int64_t> mkA, mkB, rA, rB, tA, tB, uA, uB, tiles, tot;
+  TQ_CHECK(mkA.alloc(KA, s));
+  TQ_CHECK(mkB.alloc(KB, s));
+  TQ_CUDA(cudaMemsetAsync(mkA.p, 0, KA * 8, s));
+  TQ_CUDA(cudaMemsetAsync(mkB.p, 0, KB * 8, s));
+  TQ_CHECK(rA.alloc(A->nb, s));
+  TQ_CHECK(tA.alloc(A->nb, s));
+  TQ_CHECK(uA.alloc(A->nb, s));
+  TQ_CHECK(rB.alloc(B->nb, s));
+  TQ_CHECK(tB.alloc(B->nb, s));
+  TQ_CHECK(uB.alloc(B->nb, s));
+  TQ_CHECK(tot.alloc(10, s));
+  OzSide SA = make_side(A, L.nfa, L.fa, L.nc, L.al, P->keyA.p, nullptr, nullptr, nullptr, nullptr);
+  OzSide SB = make_side(B, L.nfb, L.fb, L.nc, L.bl, P->keyB.p, nullptr, nullptr, nullptr, nullptr);
+  tc_block_stats_kernel<<<nblk(A->nb), 256, 0, s>>>(SA, OZ_M, sl, mkA.p, rA.p, tA.p, uA.p);
+  tc_block_stats_kernel<<<nblk(B->nb), 256, 0, s>>>(SB, OZ_N, sl, mkB.p, rB.p, tB.p, uB.p);
+  TQ_CUDA(cudaGetLastError());
+  TQ_CHECK(P->rowstartA.alloc(A->nb, s));
+  TQ_CHECK(P->tilestartA.alloc(A->nb, s));
+  TQ_CHECK(P->unitA.alloc(A->nb, s));
+  TQ_CHECK(P->rowstartB.alloc(B->nb, s));
+  TQ_CHECK(P->tilestartB.alloc(B->nb, s));
+  TQ_CHECK(P->unitB.alloc(B->nb, s));
+  TQ_CHECK(P->rowA.alloc(KA, s));
+  TQ_CHECK(P->rowB.alloc(KB, s));
+  TQ_CHECK(scan_exclusive(rA.p, P->rowstartA.p, A->nb, tot.p + 0, s));
+  TQ_CHECK(scan_exclusive(tA.p, P->tilestartA.p, A->nb, tot.p + 1, s));
+  TQ_CHECK(scan_exclusive(uA.p, P->unitA.p, A->nb, tot.p + 2, s));
+  TQ_CHECK(scan_exclusive(mkA.p, P->rowA.p, KA, tot.p + 3, s));
+  TQ_CHECK(scan_exclusive(rB.p, P->rowstartB.p, B->nb, tot.p + 4, s));
+  TQ_CHECK(scan_exclusive(tB.p, P->tilestartB.p, B->nb, tot.p + 5, s));
+  TQ_CHECK(scan_exclusive(uB.p, P->unitB.p, B->nb, tot.p + 6, s));
+  TQ_CHECK(scan_exclusive(mkB.p, P->rowB.p, KB, tot.p + 7, s));
+  // per-output tiles and k-steps
+  TQ_CHECK(P->nk_pair.alloc(np, s));
+  TQ_CHECK(P->ksum.alloc(no, s));
+  TQ_CHECK(tiles.alloc(no, s));
+  TQ_CHECK(P->tc_tile_start.alloc(no + 1, s));
+  tc_out_kernel<<<nblk(no), 256, 0, s>>>(A->view(), B->view(), L, P->pa.p, P->pb.p, P->seg.p,
+                                          P->perm.p, no, P->nk_pair.p, tiles.p, P->ksum.p);
+  TQ_CUDA(cudaGetLastError());
+  TQ_CHECK(scan_exclusive(tiles.p, P->tc_tile_start.p, no, tot.p + 8, s));
+  int64_t h[10];
+  int32_t h_bad = 0;
+  TQ_CUDA(cudaMemcpyAsync(h, tot.p, 9 * 8, cudaMemcpyDeviceToHost, s));
+  TQ_CUDA(cudaMemcpyAsync(&h_bad, bad.p, 4, cudaMemcpyDeviceToHost, s));
+  TQ_CUDA(cudaStreamSynchronize(s));
+  if (h_bad)
+    return fail(TQ_ERR_UNSUPPORTED,
+                "the sliced forms need sector-aligned blocks: matched blocks must cover the same "
+                "interval on every contracted leg; use the native precision");
+  P->rowsA = h[0];
+  P->tilesA = h[1];
+  P->nexpA = h[3];
+  P->rowsB = h[4];
+  P->tilesB = h[5];
+  P->nexpB = h[7];
+  P->tc_tiles = h[8];
+  TQ_CHECK(P->expA.alloc(std::max<int64_t>(P->nexpA, 1), s));
+  TQ_CHECK(P->expB.alloc(std::max<int64_t>(P->nexpB, 1), s));
+  TQ_CHECK(P->sliceA.alloc(std::max<int64_t>(h[2], 1) * 256, s));
+  TQ_CHECK(P->sliceB.alloc(std::max<int64_t>(h[6], 1) * 256, s));
+  TQ_CHECK(P->err.alloc(1, s));
+  TQ_CUDA(cudaMemsetAsync(P->err.p, 0, 4, s));
+  return TQ_OK;
+}
+
+static tq_status run_tc(tq_plan *P, const GemmJob &g, cudaStream_t s) {
+  const LegSpec &L = P->L;
+  OzSide SA = make_side(P->A, L.nfa, L.fa, L.nc, L.al, P->keyA.p, P->rowA.p, P->rowstartA.p,
+                        P->tilestartA.p, P->unitA.p);
+  OzSide SB = make_side(P->B, L.nfb, L.fb, L.nc, L.bl, P->keyB.p, P->rowB.p, P->rowstartB.p,
+                        P->tilestartB.p, P->unitB.p);
+  OzJob J;
+  J.g = g;
+  J.tile_start = P->tc_tile_start.p;
+  J.n_tiles = P->tc_tiles;
+  J.ksum = P->ksum.p;
+  J.nk_pair = P->nk_pair.p;
+  J.sliceA = P->sliceA.p;
+  J.sliceB = P->sliceB.p;
+  J.unitA = P->unitA.p;
+  J.unitB = P->unitB.p;
+  J.keyA = P->keyA.p;
+  J.keyB = P->keyB.p;
+  J.rowA = P->rowA.p;
+  J.rowB = P->rowB.p;
+  J.expA = P->expA.p;
+  J.expB = P->expB.p;
+  J.s = P->slices;
+  J.nstages = oz_stages(P->slices);
+  J.err = P->err.p;
+  return launch_ozaki(J, SA, SB, P->rowsA, P->rowsB, P->tilesA, P->tilesB, P->expA.p, P->expB.p,
+                      P->nexpA, P->nexpB, s);
+}
+
 tq_status validate_legs(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,
                         const int64_t *b_legs, LegSpec &L) {
   if (!A || !B) return fail(TQ_ERR_INVALID, "tensor is NULL");
@@ -301,20 +488,24 @@ tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64
     P->n_out = 0;
   } else {
     int64_t n_out = n_pairs;
+    P->tc = o.precision != TQ_PREC_NATIVE;
+    int64_t KA = 1, KB = 1;
+    if ((o.layout == TQ_LAYOUT_REDUCED || P->tc) && n_pairs) {
+      // interval-id keys of the free boxes: output grouping and exponent classes
+      TQ_CHECK(P->keyA.alloc(std::max<int64_t>(A->nb, 1), s));
+      TQ_CHECK(P->keyB.alloc(std::max<int64_t>(B->nb, 1), s));
+      TQ_CHECK(box_keys(A, L.nfa, L.fa, P->keyA.p, &KA, s));
+      TQ_CHECK(box_keys(B, L.nfb, L.fb, P->keyB.p, &KB, s));
+    }
     if (o.layout == TQ_LAYOUT_REDUCED && n_pairs) {
       // 3. group pairs by output box
-      DevArray<int64_t> ka, kb, key, flag, sid;
-      int64_t KA = 1, KB = 1;
-      TQ_CHECK(ka.alloc(std::max<int64_t>(A->nb, 1), s));
-      TQ_CHECK(kb.alloc(std::max<int64_t>(B->nb, 1), s));
-      TQ_CHECK(box_keys(A, L.nfa, L.fa, ka.p, &KA, s));
-      TQ_CHECK(box_keys(B, L.nfb, L.fb, kb.p, &KB, s));
+      DevArray<int64_t> key, flag, sid;
       if (KB > 0 && KA > (int64_t(1) << 62) / KB)
         return fail(TQ_ERR_UNSUPPORTED, "output box key range exceeds 2^62");
       TQ_CHECK(key.alloc(n_pairs, s));
       TQ_CHECK(P->perm.alloc(n_pairs, s));
-      pair_key_kernel<<<nblk(n_pairs), 256, 0, s>>>(P->pa.p, P->pb.p, n_pairs, ka.p, kb.p, KA,
-                                                    key.p);
+      pair_key_kernel<<<nblk(n_pairs), 256, 0, s>>>(P->pa.p, P->pb.p, n_pairs, P->keyA.p,
+                                                    P->keyB.p, KA, key.p);
       iota_kernel<<<nblk(n_pairs), 256, 0, s>>>(P->perm.p, n_pairs);
       TQ_CUDA(cudaGetLastError());
       TQ_CHECK(radix_sort_pairs(key.p, P->perm.p, n_pairs, bits_for(KA * KB), s));
@@ -358,6 +549,7 @@ tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64
     TQ_CHECK(alloc_data(C, h[2], s));
     C->host_valid = false;
     C->dev_valid = true;
+    if (P->tc && n_pairs) TQ_CHECK(plan_tc(P.get(), KA, KB, s));
   }
   P->C = C;
   Cguard.release();
@@ -383,6 +575,7 @@ tq_status plan_run(tq_plan *P, cudaStream_t s) {
     return launch_dot_native(job, P->n_pairs, P->chunk_start.p, P->n_chunks, P->partials.p,
                              P->A->dtype, s);
   if (P->n_tiles == 0) return TQ_OK;
+  if (P->tc) return run_tc(P, job, s);
   return launch_gemm_native(job, P->n_tiles, P->A->dtype, s);
 }
 
@@ -424,6 +617,14 @@ tq_status tq_bs_contract(const tq_bs *A, const tq_bs *B, int32_t n_legs, const i
   tq_bs *C = nullptr;
   TQ_CHECK(plan_build(A, B, n_legs, a_legs, b_legs, opts, (cudaStream_t)stream, &P, &C));
   tq_status st = plan_run(P, (cudaStream_t)stream);
+  if (st == TQ_OK && P->tc && P->err.p) {
+    // the tensor-core kernel's bounded waits report through this flag
+    int32_t e = 0;
+    cudaError_t ce = cudaMemcpyAsync(&e, P->err.p, 4, cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize((cudaStream_t)stream);
+    if (ce != cudaSuccess) st = cuda_fail(ce, "cudaMemcpyAsync");
+    else if (e) st = fail(TQ_ERR_TIMEOUT, "a tensor-core pipeline wait gave up (flags " + std::to_string(e) + ")");
+  }
   // the plan's scratch is released stream-ordered after the kernels that use it
   tq_plan_destroy(P);
   if (st != TQ_OK) {

@@ -18,6 +18,18 @@ struct tq_plan {
   tq::DevArray<int64_t> tile_start;       // [n_out+1]
   tq::DevArray<int64_t> chunk_start;      // rank-0 results
   tq::DevArray<double> partials;          // rank-0 results (float partials use the low half)
+  // tensor-core (sliced) forms
+  int32_t slices = 0;
+  bool tc = false;
+  tq::DevArray<int64_t> keyA, keyB;            // free-box class key per block
+  tq::DevArray<int64_t> rowA, rowB;            // per key: exponent table offset
+  tq::DevArray<int64_t> rowstartA, rowstartB;  // per block: first row
+  tq::DevArray<int64_t> tilestartA, tilestartB;
+  tq::DevArray<int64_t> unitA, unitB;          // per block: slice offset / 256 B
+  tq::DevArray<int64_t> ksum, tc_tile_start;
+  tq::DevArray<int32_t> expA, expB, nk_pair, err;
+  tq::DevArray<uint8_t> sliceA, sliceB;
+  int64_t rowsA = 0, rowsB = 0, tilesA = 0, tilesB = 0, nexpA = 0, nexpB = 0, tc_tiles = 0;
 };
 
 namespace tq {
