@@ -11,13 +11,16 @@
 //     digits d_0..d_{s-1} in [-128, 128]; slice t is stored as the bf16 value
 //     d_t * 2^(-8t) (exact: at most 8 significant bits);
 //   * the slice products A_t B_u^T with t+u <= s-1 run on the tensor cores with
-//     fp32 accumulation in TMEM, in three accumulators by t+u: D0 (t+u=0, whole
-//     numbers |.| <= K*2^14) and D1 (t+u=1, multiples of 2^-8, |.| <= K*2^7)
-//     stay exact in fp32 for K <= 512 and are flushed every 512 columns of the
-//     fused K into an exact int64 running sum S = 256*(D0 + D1) kept in TMEM;
-//     D2 (t+u >= 2, terms <= 2^-16 of D0) accumulates in fp32 over the whole K;
-//   * C = 2^(e_r + f_c - 40) * (2^16 S + round(2^24 D2)), converted to FP64
-//     with integer operations.
+//     fp32 accumulation in TMEM, in four accumulators by g = t+u: D0, D1, D2
+//     (g = 0, 1, 2) hold multiples of 2^(-8g) below (g+1) K 2^14 2^(-8g), whole
+//     numbers of 24 bits or fewer for K <= 320, so the tensor core sums them
+//     exactly; D3 (g >= 3, at most 2^-24 of D0) is rounded.  Every 320 columns
+//     of the fused K (all pairs of the output block, in order) the four are
+//     folded into an exact int64 running sum S = sum_a round(2^24 D_a) held in
+//     the epilogue's registers.  (A single fp32 accumulator for g >= 2 is not
+//     enough: the tensor core's fp32 accumulation truncates, which loses about
+//     K ulps of the g = 2 terms.)
+//   * C = S * 2^(e_r + f_c - 40), converted to FP64 with integer operations.
 // No FP64 arithmetic runs in the GEMM: GB300 issues about 2 FP64 FMAs per SM
 // per clock against ~4000 bf16 FMAs, so FP64 work stays in the row-exponent
 // pass (one ilogb per row) only.
@@ -39,8 +42,7 @@ namespace tq {
 
 constexpr int OZ_THREADS = 320;  // warp 0: loads, warp 1: MMA, warps 2-9: epilogue
 constexpr uint32_t OZ_TMEM_COLS = 512;
-constexpr uint32_t COL_D0 = 0, COL_D1 = OZ_N, COL_D2 = 2 * OZ_N, COL_SLO = 3 * OZ_N,
-                   COL_SHI = 4 * OZ_N;
+// TMEM columns: accumulator D_a (a = 0..3) at [a*OZ_N, (a+1)*OZ_N)
 constexpr int OZ_SMEM_BYTES = 200 * 1024;
 
 __device__ __forceinline__ int64_t oz_find(const int64_t *start, int64_t n, int64_t t) {
@@ -310,8 +312,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
         oz_decode(J, t, T);
         const uint32_t idesc = idesc_bf16_f32(OZ_M, (uint32_t)T.nmma);
         int kc = 0;
-        bool tile_first = true;
-        bool fresh0 = true, fresh1 = true, fresh2 = true;
+        uint32_t fresh = 0xf;  // bit a: accumulator D_a not yet written in this chunk
         for (int64_t sidx = T.seg0; sidx < T.seg1 && !abort_flag; sidx++) {
           const int64_t p = J.g.perm ? J.g.perm[sidx] : sidx;
           const int64_t nk = J.nk_pair[p];
@@ -330,8 +331,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
                 break;
               }
               tc_fence_after();
-              fresh0 = fresh1 = true;
-              if (tile_first) fresh2 = true;
+              fresh = 0xf;
             }
             const uint32_t sa = smem_u32(smem + st * stage_bytes);
             const uint32_t sb = sa + a_bytes_max;
@@ -339,13 +339,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
               const uint64_t da = smem_desc(sa + ta * T.ga * 256, 128, 256);
               for (int ub = 0; ub < s - ta; ub++) {
                 const uint64_t db = smem_desc(sb + ub * T.gb * 256, 128, 256);
-                const int g = ta + ub;
-                uint32_t col;
-                bool fresh;
-                if (g == 0) { col = COL_D0; fresh = fresh0; fresh0 = false; }
-                else if (g == 1) { col = COL_D1; fresh = fresh1; fresh1 = false; }
-                else { col = COL_D2; fresh = fresh2; fresh2 = false; }
-                mma_bf16(tmem + col, da, db, idesc, fresh ? 0u : 1u);
+                const int acc = ta + ub < 3 ? ta + ub : 3;
+                mma_bf16(tmem + acc * OZ_N, da, db, idesc, (fresh >> acc) & 1 ? 0u : 1u);
+                fresh &= ~(1u << acc);
               }
             }
             mma_commit(&empty_bar[st]);
@@ -353,7 +349,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
               mma_commit(&acc_full);
               f++;
               kc = 0;
-              tile_first = false;
             }
           }
         }
@@ -373,6 +368,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
     const int row = 32 * q4 + lane;
     const uint32_t lane_addr = tmem + ((uint32_t)(32 * q4) << 16);
     const int cbase = half * (OZ_N / 2);
+    const int n_acc = s < 4 ? s : 4;  // accumulators the slice products reach
     uint32_t f = 0;
     for (int64_t t = blockIdx.x; t < J.n_tiles && !abort_flag; t += gridDim.x) {
       OzTile T;
@@ -381,6 +377,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
       const int64_t grow = T.mt * OZ_M + row;
       const bool row_ok = grow < T.m;
       const int er = row_ok ? J.expA[J.rowA[J.keyA[T.i0]] + grow] : 0;
+      // S: running sum in units of 2^-24 of the leading slice product, exact
+      long long S[OZ_N / 2];
+#pragma unroll
+      for (int y = 0; y < OZ_N / 2; y++) S[y] = 0;
       for (int64_t c = 0; c < nflush; c++, f++) {
         if (!mbar_wait(&acc_full, f & 1)) {
           atomicOr(J.err, 16);
@@ -388,64 +388,36 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
           break;
         }
         tc_fence_after();
-        const bool last = c == nflush - 1;
-        if (!last) {
-          // fold the exact partials D0, D1 into the int64 running sum S
-#pragma unroll 1
-          for (int x = 0; x < OZ_N / 32; x++) {
-            uint32_t d0[16], d1[16], lo[16], hi[16];
-            tmem_ld16(lane_addr + COL_D0 + cbase + 16 * x, d0);
-            tmem_ld16(lane_addr + COL_D1 + cbase + 16 * x, d1);
-            if (c > 0) {
-              tmem_ld16(lane_addr + COL_SLO + cbase + 16 * x, lo);
-              tmem_ld16(lane_addr + COL_SHI + cbase + 16 * x, hi);
-            }
+        // D0..D2 hold whole multiples of 2^-24 below 2^24 (exact); D3 is rounded
+#pragma unroll
+        for (int x = 0; x < OZ_N / 32; x++) {
+#pragma unroll
+          for (int a = 0; a < 4; a++) {
+            if (a >= n_acc) break;
+            uint32_t v[16];
+            tmem_ld16(lane_addr + a * OZ_N + cbase + 16 * x, v);
             tmem_ld_wait();
 #pragma unroll
-            for (int y = 0; y < 16; y++) {
-              long long sv = c > 0 ? (long long)(((unsigned long long)hi[y] << 32) | lo[y]) : 0;
-              sv += 256ll * __float2ll_rn(__uint_as_float(d0[y])) +
-                    __float2ll_rn(__uint_as_float(d1[y]) * 256.0f);
-              lo[y] = (uint32_t)(unsigned long long)sv;
-              hi[y] = (uint32_t)((unsigned long long)sv >> 32);
-            }
-            tmem_st16(lane_addr + COL_SLO + cbase + 16 * x, lo);
-            tmem_st16(lane_addr + COL_SHI + cbase + 16 * x, hi);
+            for (int y = 0; y < 16; y++)
+              S[16 * x + y] += __float2ll_rn(__uint_as_float(v[y]) * 16777216.0f);
           }
-          tmem_st_wait();
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&acc_empty);
-        } else {
-          double *C = (double *)J.g.C + J.g.c_off[T.o];
-#pragma unroll 1
-          for (int x = 0; x < OZ_N / 32; x++) {
-            uint32_t d0[16], d1[16], d2[16], lo[16], hi[16];
-            tmem_ld16(lane_addr + COL_D0 + cbase + 16 * x, d0);
-            tmem_ld16(lane_addr + COL_D1 + cbase + 16 * x, d1);
-            tmem_ld16(lane_addr + COL_D2 + cbase + 16 * x, d2);
-            if (c > 0) {
-              tmem_ld16(lane_addr + COL_SLO + cbase + 16 * x, lo);
-              tmem_ld16(lane_addr + COL_SHI + cbase + 16 * x, hi);
-            }
-            tmem_ld_wait();
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty);
+      }
+      if (abort_flag) break;
+      // C = S * 2^(e_r + f_c - 40)
+      double *C = (double *)J.g.C + J.g.c_off[T.o];
+      const int64_t *rowB = J.rowB + J.keyB[T.j0];
+      if (row_ok) {
 #pragma unroll
-            for (int y = 0; y < 16; y++) {
-              const int64_t gcol = T.nt * OZ_N + cbase + 16 * x + y;
-              long long sv = c > 0 ? (long long)(((unsigned long long)hi[y] << 32) | lo[y]) : 0;
-              sv += 256ll * __float2ll_rn(__uint_as_float(d0[y])) +
-                    __float2ll_rn(__uint_as_float(d1[y]) * 256.0f);
-              const long long tv =
-                  sv * 65536ll + __float2ll_rn(__uint_as_float(d2[y]) * 16777216.0f);
-              if (row_ok && gcol < T.n) {
-                const int fc = J.expB[J.rowB[J.keyB[T.j0]] + gcol];
-                C[grow + gcol * T.m] = oz_i64_ldexp(tv, er + fc - 40);
-              }
-            }
+        for (int y = 0; y < OZ_N / 2; y++) {
+          const int64_t gcol = T.nt * OZ_N + cbase + y;
+          if (gcol < T.n) {
+            const int fc = J.expB[*rowB + gcol];
+            C[grow + gcol * T.m] = oz_i64_ldexp(S[y], er + fc - 40);
           }
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&acc_empty);
         }
       }
     }
