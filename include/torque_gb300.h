@@ -167,6 +167,14 @@ tq_status tq_plan_create(const tq_bs *A, const tq_bs *B, int32_t n_legs,
 tq_status tq_plan_execute(tq_plan *plan, tq_stream stream);
 /* Useful flops of the plan: sum over matched block pairs of 2*m*n*k. */
 tq_status tq_plan_flops(const tq_plan *plan, double *flops, int64_t *n_pairs);
+/* Record CUDA events on the launching stream around the phases of each
+ * tq_plan_execute (operand preparation, block GEMM). */
+tq_status tq_plan_set_profiling(tq_plan *plan, int32_t enable);
+/* Durations of the last profiled execute; synchronises on its last event. */
+tq_status tq_plan_last_timings(tq_plan *plan, float *prepare_ms, float *gemm_ms);
+/* Status of the tensor-core kernel's bounded waits in the last execute
+ * (synchronises the stream): TQ_OK or TQ_ERR_TIMEOUT. */
+tq_status tq_plan_check(tq_plan *plan, tq_stream stream);
 tq_status tq_plan_destroy(tq_plan *plan);
 
 /* ---- errors and hooks -------------------------------------------------- */
@@ -177,6 +185,9 @@ const char *tq_last_error_string(void);
 /* Test hook: the next `after` device allocations succeed, then every one is
  * refused with TQ_ERR_OOM until reset with after < 0. */
 void tq_debug_fail_alloc_after(int64_t after);
+
+/* Kernels the library has launched in this process so far. */
+int64_t tq_debug_kernel_launches(void);
 
 #ifdef __cplusplus
 }

@@ -26,7 +26,7 @@ _SRC = os.path.join(_HERE, "torque_oracle.c")
 def build(force: bool = False) -> str:
     """Compile the C oracle with gcc (x86_64 or aarch64; no flags that differ)."""
     if force or not os.path.exists(_SO) or os.path.getmtime(_SO) < os.path.getmtime(_SRC):
-        cmd = ["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-o", _SO, _SRC]
+        cmd = ["gcc", "-O2", "-std=c99", "-fopenmp", "-fPIC", "-shared", "-o", _SO, _SRC]
         subprocess.check_call(cmd)
     return _SO
 
@@ -73,7 +73,29 @@ def lib():
         _lib.orc_densify.argtypes = [PB, PD]
         _lib.orc_hard_transpose.restype = None
         _lib.orc_hard_transpose.argtypes = [PB, P64, PD]
+        _lib.orc_pairs_baseline.restype = ctypes.c_int32
+        _lib.orc_pairs_baseline.argtypes = [PB, PB, ctypes.c_int32, P64, P64, ctypes.c_int64,
+                                            P64, P64, P64, PD]
     return _lib
+
+
+def pairs_baseline(A: HostBS, B: HostBS, pairs, pa, pb):
+    """The reference CPU path's per-pair work (gather + dense multiply) for the
+    given pairs, OpenMP-parallel over pairs.  Returns (blocks, threads used)."""
+    al, bl, nc = _legs(pairs)
+    pa = np.ascontiguousarray(pa, dtype=np.int64)
+    pb = np.ascontiguousarray(pb, dtype=np.int64)
+    fa = [l for l in range(A.rank) if l not in set(al.tolist())]
+    fb = [l for l in range(B.rank) if l not in set(bl.tolist())]
+    m = np.prod(A.block_dims[pa][:, fa], axis=1) if fa else np.ones(pa.size, np.int64)
+    n = np.prod(B.block_dims[pb][:, fb], axis=1) if fb else np.ones(pb.size, np.int64)
+    sizes = (m * n).astype(np.int64)
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    out = np.zeros(max(int(sizes.sum()), 1), np.float64)
+    ca, cb = A.c(), B.c()
+    threads = lib().orc_pairs_baseline(ctypes.byref(ca), ctypes.byref(cb), nc, _p64(al), _p64(bl),
+                                       pa.size, _p64(pa), _p64(pb), _p64(offs), _pd(out))
+    return out, offs, threads
 
 
 def _p64(a):

@@ -8,6 +8,9 @@
 
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define MAXR 32
 
@@ -178,6 +181,74 @@ int32_t orc_pair_values(const orc_bs *A, const orc_bs *B, int32_t nc,
     }
   free(ra); free(rb); free(ka); free(kb);
   return ORC_OK;
+}
+
+/* Gather the sub-box of block b (rows over free legs fl, columns over the
+ * contracted legs cl restricted to [cb, ce]) into a contiguous row-major
+ * rows x K matrix, as sort_into_matrix does. */
+static void gather_rep(const orc_bs *T, int64_t b, int nf, const int *fl, int nc,
+                       const int64_t *cl, const int64_t *cb, const int64_t *ce, double *out,
+                       int64_t *rows_out, int64_t *k_out) {
+  const int64_t *bb = T->begin + b * T->rank, *be = T->end + b * T->rank;
+  const int64_t *st = T->strides + b * T->rank;
+  int64_t base = T->offsets[b], rows = 1, K = 1, rd[MAXR], kd[MAXR];
+  for (int q = 0; q < nf; q++) { rd[q] = be[fl[q]] - bb[fl[q]] + 1; rows *= rd[q]; }
+  for (int k = 0; k < nc; k++) {
+    kd[k] = ce[k] - cb[k] + 1;
+    K *= kd[k];
+    base += (cb[k] - bb[cl[k]]) * st[cl[k]];
+  }
+  for (int64_t r = 0; r < rows; r++) {
+    int64_t t = r, ra = base;
+    for (int q = 0; q < nf; q++) { ra += (t % rd[q]) * st[fl[q]]; t /= rd[q]; }
+    for (int64_t c = 0; c < K; c++) {
+      int64_t u = c, a = ra;
+      for (int k = 0; k < nc; k++) { a += (u % kd[k]) * st[cl[k]]; u /= kd[k]; }
+      out[r * K + c] = T->data[a];
+    }
+  }
+  *rows_out = rows;
+  *k_out = K;
+}
+
+int32_t orc_pairs_baseline(const orc_bs *A, const orc_bs *B, int32_t nc, const int64_t *al,
+                           const int64_t *bl, int64_t n, const int64_t *pa, const int64_t *pb,
+                           const int64_t *out_offsets, double *out) {
+  int fa[MAXR], fb[MAXR];
+  const int nfa = free_legs(A->rank, nc, al, fa);
+  const int nfb = free_legs(B->rank, nc, bl, fb);
+  int32_t threads = 1;
+#ifdef _OPENMP
+#pragma omp parallel
+  {
+#pragma omp single
+    threads = omp_get_num_threads();
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int64_t q = 0; q < n; q++) {
+    int64_t cb[MAXR], ce[MAXR], m, n_, K, K2;
+    orc_pair_boxes(A, B, nc, al, bl, pa[q], pb[q], NULL, NULL, cb, ce, NULL, NULL, NULL, NULL);
+    int64_t mm = 1, nn = 1, kk = 1;
+    for (int x = 0; x < nfa; x++) mm *= A->end[pa[q] * A->rank + fa[x]] - A->begin[pa[q] * A->rank + fa[x]] + 1;
+    for (int x = 0; x < nfb; x++) nn *= B->end[pb[q] * B->rank + fb[x]] - B->begin[pb[q] * B->rank + fb[x]] + 1;
+    for (int k = 0; k < nc; k++) kk *= ce[k] - cb[k] + 1;
+    double *ra = (double *)malloc(sizeof(double) * (size_t)(mm * kk));
+    double *rb = (double *)malloc(sizeof(double) * (size_t)(nn * kk));
+    gather_rep(A, pa[q], nfa, fa, nc, al, cb, ce, ra, &m, &K);
+    gather_rep(B, pb[q], nfb, fb, nc, bl, cb, ce, rb, &n_, &K2);
+    double *c = out + out_offsets[q];
+    for (int64_t j = 0; j < n_; j++)
+      for (int64_t i = 0; i < m; i++) {
+        const double *x = ra + i * K, *y = rb + j * K;
+        double s = 0.0;
+        for (int64_t k = 0; k < K; k++) s += x[k] * y[k];
+        c[i + j * m] = s;
+      }
+    free(ra);
+    free(rb);
+  }
+  return threads;
 }
 
 int64_t orc_contract_size(const orc_bs *A, const orc_bs *B, int32_t nc,

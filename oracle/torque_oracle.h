@@ -106,6 +106,18 @@ int32_t orc_contract(const orc_bs *A, const orc_bs *B, int32_t nc,
                      int64_t *out_begin, int64_t *out_end, int64_t *out_offsets,
                      double *out_data);
 
+/*
+ * The CPU baseline: the reference CPU path's per-pair work for a list of pairs,
+ * in parallel over pairs (OpenMP).  For each pair the two sub-blocks are first
+ * gathered into contiguous matrices A_rep (m x k) and B_rep (n x k), as
+ * sort_into_matrix does (src/tensor/block_sparse.h:17-80, :527-539), then
+ * C = A_rep B_rep^T is formed in double (block_sparse.h:541-542).  out_offsets[q]
+ * is where pair q's m x n column-major block goes.  Returns the thread count.
+ */
+int32_t orc_pairs_baseline(const orc_bs *A, const orc_bs *B, int32_t nc, const int64_t *a_legs,
+                           const int64_t *b_legs, int64_t n, const int64_t *pa,
+                           const int64_t *pb, const int64_t *out_offsets, double *out);
+
 /* query: sum over every block containing idx (src/tensor/block_sparse.h:373-409). */
 double orc_query(const orc_bs *T, const int64_t *idx);
 

@@ -118,6 +118,17 @@ def test_small_u1_dense_parity():
     assert np.max(np.abs(d1 - data)) <= 1e-13 * np.max(np.abs(data))
 
 
+def test_cpu_baseline_port_matches_oracle():
+    """The timed CPU baseline (gather into matrices, then multiply) gives the
+    reference-layout values of the accurate oracle to rounding."""
+    c, A, B = small_host()
+    pa, pb = orc.match(A, B, c.pairs)
+    out, offs, threads = orc.pairs_baseline(A, B, c.pairs, pa, pb)
+    ob, oe, off, want = orc.contract(A, B, c.pairs, mode=0)
+    assert np.array_equal(offs, off) and threads >= 1
+    assert np.max(np.abs(out - want)) <= 1e-13 * np.max(np.abs(want))
+
+
 def test_reference_cpu_stride_defect():
     """The reference CPU path reads element strides from column j_block of each
     tensor's index tables (src/tensor/block_sparse.h:531,538).  With uneven blocks

@@ -50,8 +50,13 @@ SIGNATURES = {
     "tq_plan_execute": (ST, [P, P]),
     "tq_plan_flops": (ST, [P, ctypes.POINTER(ctypes.c_double), P64]),
     "tq_plan_destroy": (ST, [P]),
+    "tq_plan_set_profiling": (ST, [P, I32]),
+    "tq_plan_last_timings": (ST, [P, ctypes.POINTER(ctypes.c_float),
+                                  ctypes.POINTER(ctypes.c_float)]),
+    "tq_plan_check": (ST, [P, P]),
     "tq_last_error_string": (ctypes.c_char_p, []),
     "tq_debug_fail_alloc_after": (None, [I64]),
+    "tq_debug_kernel_launches": (I64, []),
 }
 
 

@@ -272,6 +272,21 @@ class ContractionPlan:
         check(load().tq_plan_execute(self._p, _stream(stream)))
         return self.result
 
+    def check(self, stream=None):
+        """Raise if a bounded device wait of the last execute gave up (syncs)."""
+        check(load().tq_plan_check(self._p, _stream(stream)))
+
+    def set_profiling(self, enable: bool = True):
+        check(load().tq_plan_set_profiling(self._p, 1 if enable else 0))
+
+    def last_timings(self):
+        """(prepare_ms, gemm_ms) of the last profiled execute, from CUDA events
+        recorded on the launching stream."""
+        a = ctypes.c_float()
+        b = ctypes.c_float()
+        check(load().tq_plan_last_timings(self._p, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     @property
     def flops(self) -> float:
         f = ctypes.c_double()

@@ -161,17 +161,17 @@ static tq_status box_keys(const tq_bs *T, int32_t nlegs, const int32_t *legs, in
     TQ_CUDA(cudaMemsetAsync(emax.p, 0, dim * 8, s));
     TQ_CUDA(cudaMemsetAsync(bad.p, 0, 4, s));
     const DevBS v = T->view();
-    mark_intervals_kernel<<<nblk(T->nb), 256, 0, s>>>(v, leg, is_begin.p, emin.p, emax.p);
+    count_launch(), mark_intervals_kernel<<<nblk(T->nb), 256, 0, s>>>(v, leg, is_begin.p, emin.p, emax.p);
     TQ_CHECK(scan_exclusive(is_begin.p, ids.p, dim, total.p, s));
-    check_intervals_kernel<<<nblk(dim), 256, 0, s>>>(is_begin.p, ids.p, dim, emin.p, emax.p,
+    count_launch(), check_intervals_kernel<<<nblk(dim), 256, 0, s>>>(is_begin.p, ids.p, dim, emin.p, emax.p,
                                                      begin_of_id.p, bad.p);
     int64_t n_ids = 0;
     int32_t h_bad = 0;
     TQ_CUDA(cudaMemcpyAsync(&n_ids, total.p, 8, cudaMemcpyDeviceToHost, s));
     TQ_CUDA(cudaStreamSynchronize(s));
-    check_disjoint_kernel<<<nblk(std::max<int64_t>(n_ids, 1)), 256, 0, s>>>(begin_of_id.p, n_ids,
+    count_launch(), check_disjoint_kernel<<<nblk(std::max<int64_t>(n_ids, 1)), 256, 0, s>>>(begin_of_id.p, n_ids,
                                                                            emax.p, bad.p);
-    block_key_kernel<<<nblk(T->nb), 256, 0, s>>>(v, leg, ids.p, radix, key);
+    count_launch(), block_key_kernel<<<nblk(T->nb), 256, 0, s>>>(v, leg, ids.p, radix, key);
     TQ_CUDA(cudaGetLastError());
     TQ_CUDA(cudaMemcpyAsync(&h_bad, bad.p, 4, cudaMemcpyDeviceToHost, s));
     TQ_CUDA(cudaStreamSynchronize(s));
@@ -280,7 +280,7 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   DevArray<int32_t> bad;
   TQ_CHECK(bad.alloc(1, s));
   TQ_CUDA(cudaMemsetAsync(bad.p, 0, 4, s));
-  tc_align_kernel<<<nblk(np), 256, 0, s>>>(A->view(), B->view(), L, P->pa.p, P->pb.p, np, bad.p);
+  count_launch(), tc_align_kernel<<<nblk(np), 256, 0, s>>>(A->view(), B->view(), L, P->pa.p, P->pb.p, np, bad.p);
   TQ_CUDA(cudaGetLastError());
   // per-block geometry of both sides
   DevArray<int64_t> mkA, mkB, rA, rB, tA, tB, uA, uB, tiles, tot;
@@ -297,8 +297,8 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   TQ_CHECK(tot.alloc(10, s));
   OzSide SA = make_side(A, L.nfa, L.fa, L.nc, L.al, P->keyA.p, nullptr, nullptr, nullptr, nullptr);
   OzSide SB = make_side(B, L.nfb, L.fb, L.nc, L.bl, P->keyB.p, nullptr, nullptr, nullptr, nullptr);
-  tc_block_stats_kernel<<<nblk(A->nb), 256, 0, s>>>(SA, OZ_M, sl, mkA.p, rA.p, tA.p, uA.p);
-  tc_block_stats_kernel<<<nblk(B->nb), 256, 0, s>>>(SB, OZ_N, sl, mkB.p, rB.p, tB.p, uB.p);
+  count_launch(), tc_block_stats_kernel<<<nblk(A->nb), 256, 0, s>>>(SA, OZ_M, sl, mkA.p, rA.p, tA.p, uA.p);
+  count_launch(), tc_block_stats_kernel<<<nblk(B->nb), 256, 0, s>>>(SB, OZ_N, sl, mkB.p, rB.p, tB.p, uB.p);
   TQ_CUDA(cudaGetLastError());
   TQ_CHECK(P->rowstartA.alloc(A->nb, s));
   TQ_CHECK(P->tilestartA.alloc(A->nb, s));
@@ -321,7 +321,7 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   TQ_CHECK(P->ksum.alloc(no, s));
   TQ_CHECK(tiles.alloc(no, s));
   TQ_CHECK(P->tc_tile_start.alloc(no + 1, s));
-  tc_out_kernel<<<nblk(no), 256, 0, s>>>(A->view(), B->view(), L, P->pa.p, P->pb.p, P->seg.p,
+  count_launch(), tc_out_kernel<<<nblk(no), 256, 0, s>>>(A->view(), B->view(), L, P->pa.p, P->pb.p, P->seg.p,
                                           P->perm.p, no, P->nk_pair.p, tiles.p, P->ksum.p);
   TQ_CUDA(cudaGetLastError());
   TQ_CHECK(scan_exclusive(tiles.p, P->tc_tile_start.p, no, tot.p + 8, s));
@@ -375,8 +375,10 @@ static tq_status run_tc(tq_plan *P, const GemmJob &g, cudaStream_t s) {
   J.s = P->slices;
   J.nstages = oz_stages(P->slices);
   J.err = P->err.p;
-  return launch_ozaki(J, SA, SB, P->rowsA, P->rowsB, P->tilesA, P->tilesB, P->expA.p, P->expB.p,
-                      P->nexpA, P->nexpB, s);
+  TQ_CHECK(launch_ozaki_prepare(J, SA, SB, P->rowsA, P->rowsB, P->tilesA, P->tilesB, P->expA.p,
+                                P->expB.p, P->nexpA, P->nexpB, s));
+  if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[1], s));
+  return launch_ozaki_gemm(J, s);
 }
 
 tq_status validate_legs(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,
@@ -463,7 +465,7 @@ tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64
     TQ_CHECK(P->chunk_start.alloc(std::max<int64_t>(n_pairs, 1), s));
   }
   if (n_pairs) {
-    pair_stats_kernel<<<nblk(n_pairs), 256, 0, s>>>(Av, Bv, L, P->pa.p, P->pb.p, n_pairs, mnk.p,
+    count_launch(), pair_stats_kernel<<<nblk(n_pairs), 256, 0, s>>>(Av, Bv, L, P->pa.p, P->pb.p, n_pairs, mnk.p,
                                                      rc == 0 ? chunks.p : nullptr);
     TQ_CUDA(cudaGetLastError());
   }
@@ -504,23 +506,23 @@ tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64
         return fail(TQ_ERR_UNSUPPORTED, "output box key range exceeds 2^62");
       TQ_CHECK(key.alloc(n_pairs, s));
       TQ_CHECK(P->perm.alloc(n_pairs, s));
-      pair_key_kernel<<<nblk(n_pairs), 256, 0, s>>>(P->pa.p, P->pb.p, n_pairs, P->keyA.p,
+      count_launch(), pair_key_kernel<<<nblk(n_pairs), 256, 0, s>>>(P->pa.p, P->pb.p, n_pairs, P->keyA.p,
                                                     P->keyB.p, KA, key.p);
-      iota_kernel<<<nblk(n_pairs), 256, 0, s>>>(P->perm.p, n_pairs);
+      count_launch(), iota_kernel<<<nblk(n_pairs), 256, 0, s>>>(P->perm.p, n_pairs);
       TQ_CUDA(cudaGetLastError());
       TQ_CHECK(radix_sort_pairs(key.p, P->perm.p, n_pairs, bits_for(KA * KB), s));
       TQ_CHECK(flag.alloc(n_pairs, s));
       TQ_CHECK(sid.alloc(n_pairs, s));
-      seg_flag_kernel<<<nblk(n_pairs), 256, 0, s>>>(key.p, n_pairs, flag.p);
+      count_launch(), seg_flag_kernel<<<nblk(n_pairs), 256, 0, s>>>(key.p, n_pairs, flag.p);
       TQ_CHECK(scan_exclusive(flag.p, sid.p, n_pairs, tot.p + 3, s));
       TQ_CUDA(cudaMemcpyAsync(&n_out, tot.p + 3, 8, cudaMemcpyDeviceToHost, s));
       TQ_CUDA(cudaStreamSynchronize(s));
       TQ_CHECK(P->seg.alloc(n_out + 1, s));
-      seg_start_kernel<<<nblk(n_pairs), 256, 0, s>>>(flag.p, sid.p, n_pairs, n_out, P->seg.p);
+      count_launch(), seg_start_kernel<<<nblk(n_pairs), 256, 0, s>>>(flag.p, sid.p, n_pairs, n_out, P->seg.p);
       TQ_CUDA(cudaGetLastError());
     } else {
       TQ_CHECK(P->seg.alloc(n_pairs + 1, s));
-      iota_kernel<<<nblk(n_pairs + 1), 256, 0, s>>>(P->seg.p, n_pairs + 1);
+      count_launch(), iota_kernel<<<nblk(n_pairs + 1), 256, 0, s>>>(P->seg.p, n_pairs + 1);
       TQ_CUDA(cudaGetLastError());
     }
     P->n_out = n_out;
@@ -533,7 +535,7 @@ tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64
     TQ_CHECK(P->tile_start.alloc(n_out + 1, s));
     if (n_out) {
       int64_t *cb = C->d_meta.p, *ce = cb + n_out * rc, *cs = ce + n_out * rc;
-      out_meta_kernel<<<nblk(n_out), 256, 0, s>>>(Av, Bv, L, P->pa.p, P->pb.p, P->seg.p,
+      count_launch(), out_meta_kernel<<<nblk(n_out), 256, 0, s>>>(Av, Bv, L, P->pa.p, P->pb.p, P->seg.p,
                                                   P->perm.p, n_out, rc, cb, ce, cs, n_elem.p,
                                                   tiles.p);
       TQ_CUDA(cudaGetLastError());
@@ -571,12 +573,31 @@ tq_status plan_run(tq_plan *P, cudaStream_t s) {
   job.c_off = P->C->d_meta.p ? P->C->d_meta.p + 3 * P->n_out * P->C->rank : nullptr;
   job.C = P->C->data;
   job.n_out = P->n_out;
-  if (P->C->rank == 0)
-    return launch_dot_native(job, P->n_pairs, P->chunk_start.p, P->n_chunks, P->partials.p,
-                             P->A->dtype, s);
-  if (P->n_tiles == 0) return TQ_OK;
-  if (P->tc) return run_tc(P, job, s);
-  return launch_gemm_native(job, P->n_tiles, P->A->dtype, s);
+  if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[0], s));
+  tq_status st = TQ_OK;
+  if (P->C->rank == 0) {
+    if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[1], s));
+    st = launch_dot_native(job, P->n_pairs, P->chunk_start.p, P->n_chunks, P->partials.p,
+                           P->A->dtype, s);
+  } else if (P->tc && P->n_tiles) {
+    st = run_tc(P, job, s);
+  } else {
+    if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[1], s));
+    if (P->n_tiles) st = launch_gemm_native(job, P->n_tiles, P->A->dtype, s);
+  }
+  if (st == TQ_OK && P->profile) TQ_CUDA(cudaEventRecord(P->ev[2], s));
+  return st;
+}
+
+tq_status plan_check(tq_plan *P, cudaStream_t s) {
+  if (!P->tc || !P->err.p) return TQ_OK;
+  int32_t e = 0;
+  TQ_CUDA(cudaMemcpyAsync(&e, P->err.p, 4, cudaMemcpyDeviceToHost, s));
+  TQ_CUDA(cudaStreamSynchronize(s));
+  if (e)
+    return fail(TQ_ERR_TIMEOUT,
+                "a tensor-core pipeline wait gave up (flags " + std::to_string(e) + ")");
+  return TQ_OK;
 }
 
 }  // namespace tq
@@ -609,6 +630,32 @@ tq_status tq_plan_destroy(tq_plan *plan) {
   return TQ_OK;
 }
 
+tq_status tq_plan_set_profiling(tq_plan *plan, int32_t enable) {
+  if (!plan) return fail(TQ_ERR_INVALID, "plan is NULL");
+  if (enable)
+    for (auto &e : plan->ev)
+      if (!e) TQ_CUDA(cudaEventCreate(&e));
+  plan->profile = enable != 0;
+  return TQ_OK;
+}
+
+tq_status tq_plan_last_timings(tq_plan *plan, float *prepare_ms, float *gemm_ms) {
+  if (!plan) return fail(TQ_ERR_INVALID, "plan is NULL");
+  if (!plan->profile) return fail(TQ_ERR_INVALID, "profiling is off for this plan");
+  TQ_CUDA(cudaEventSynchronize(plan->ev[2]));
+  float a = 0.f, b = 0.f;
+  TQ_CUDA(cudaEventElapsedTime(&a, plan->ev[0], plan->ev[1]));
+  TQ_CUDA(cudaEventElapsedTime(&b, plan->ev[1], plan->ev[2]));
+  if (prepare_ms) *prepare_ms = a;
+  if (gemm_ms) *gemm_ms = b;
+  return TQ_OK;
+}
+
+tq_status tq_plan_check(tq_plan *plan, tq_stream stream) {
+  if (!plan) return fail(TQ_ERR_INVALID, "plan is NULL");
+  return plan_check(plan, (cudaStream_t)stream);
+}
+
 tq_status tq_bs_contract(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,
                          const int64_t *b_legs, const tq_contract_opts *opts, tq_stream stream,
                          tq_bs **out) {
@@ -617,14 +664,8 @@ tq_status tq_bs_contract(const tq_bs *A, const tq_bs *B, int32_t n_legs, const i
   tq_bs *C = nullptr;
   TQ_CHECK(plan_build(A, B, n_legs, a_legs, b_legs, opts, (cudaStream_t)stream, &P, &C));
   tq_status st = plan_run(P, (cudaStream_t)stream);
-  if (st == TQ_OK && P->tc && P->err.p) {
-    // the tensor-core kernel's bounded waits report through this flag
-    int32_t e = 0;
-    cudaError_t ce = cudaMemcpyAsync(&e, P->err.p, 4, cudaMemcpyDeviceToHost, (cudaStream_t)stream);
-    if (ce == cudaSuccess) ce = cudaStreamSynchronize((cudaStream_t)stream);
-    if (ce != cudaSuccess) st = cuda_fail(ce, "cudaMemcpyAsync");
-    else if (e) st = fail(TQ_ERR_TIMEOUT, "a tensor-core pipeline wait gave up (flags " + std::to_string(e) + ")");
-  }
+  // the tensor-core kernel's bounded waits report through a device flag
+  if (st == TQ_OK) st = plan_check(P, (cudaStream_t)stream);
   // the plan's scratch is released stream-ordered after the kernels that use it
   tq_plan_destroy(P);
   if (st != TQ_OK) {

@@ -130,9 +130,9 @@ tq_status launch_gemm_native(const GemmJob &job, int64_t n_tiles, tq_dtype dt, c
   for (int64_t base = 0; base < n_tiles; base += max_grid) {
     const unsigned g = (unsigned)std::min<int64_t>(max_grid, n_tiles - base);
     if (dt == TQ_F64)
-      gemm_native_kernel<double><<<g, NT_THREADS, 0, s>>>(job, base);
+      count_launch(), gemm_native_kernel<double><<<g, NT_THREADS, 0, s>>>(job, base);
     else
-      gemm_native_kernel<float><<<g, NT_THREADS, 0, s>>>(job, base);
+      count_launch(), gemm_native_kernel<float><<<g, NT_THREADS, 0, s>>>(job, base);
     TQ_CUDA(cudaGetLastError());
   }
   return TQ_OK;
@@ -200,14 +200,14 @@ tq_status launch_dot_native(const GemmJob &job, int64_t n_pairs, const int64_t *
     return TQ_OK;
   }
   if (dt == TQ_F64) {
-    dot_chunks_kernel<double><<<(unsigned)n_chunks, NT_THREADS, 0, s>>>(job, n_pairs, chunk_start,
+    count_launch(), dot_chunks_kernel<double><<<(unsigned)n_chunks, NT_THREADS, 0, s>>>(job, n_pairs, chunk_start,
                                                                         (double *)partials);
-    sum_partials_kernel<double><<<1, NT_THREADS, 0, s>>>((const double *)partials, n_chunks,
+    count_launch(), sum_partials_kernel<double><<<1, NT_THREADS, 0, s>>>((const double *)partials, n_chunks,
                                                          (double *)job.C);
   } else {
-    dot_chunks_kernel<float><<<(unsigned)n_chunks, NT_THREADS, 0, s>>>(job, n_pairs, chunk_start,
+    count_launch(), dot_chunks_kernel<float><<<(unsigned)n_chunks, NT_THREADS, 0, s>>>(job, n_pairs, chunk_start,
                                                                        (float *)partials);
-    sum_partials_kernel<float><<<1, NT_THREADS, 0, s>>>((const float *)partials, n_chunks,
+    count_launch(), sum_partials_kernel<float><<<1, NT_THREADS, 0, s>>>((const float *)partials, n_chunks,
                                                         (float *)job.C);
   }
   TQ_CUDA(cudaGetLastError());

@@ -11,15 +11,16 @@
 //     digits d_0..d_{s-1} in [-128, 128]; slice t is stored as the bf16 value
 //     d_t * 2^(-8t) (exact: at most 8 significant bits);
 //   * the slice products A_t B_u^T with t+u <= s-1 run on the tensor cores with
-//     fp32 accumulation in TMEM, in four accumulators by g = t+u: D0, D1, D2
-//     (g = 0, 1, 2) hold multiples of 2^(-8g) below (g+1) K 2^14 2^(-8g), whole
-//     numbers of 24 bits or fewer for K <= 320, so the tensor core sums them
-//     exactly; D3 (g >= 3, at most 2^-24 of D0) is rounded.  Every 320 columns
-//     of the fused K (all pairs of the output block, in order) the four are
-//     folded into an exact int64 running sum S = sum_a round(2^24 D_a) held in
-//     the epilogue's registers.  (A single fp32 accumulator for g >= 2 is not
+//     fp32 accumulation in TMEM, in five accumulators by g = t+u: D0..D3
+//     (g = 0..3) hold multiples of 2^(-8g) below (g+1) K 2^14 2^(-8g), whole
+//     numbers of 24 bits or fewer for K <= 240, so the tensor core sums them
+//     exactly; D4 (g >= 4, at most 2^-32 of D0) is rounded.  Every 240 columns
+//     of the fused K (all pairs of the output block, in order) the five are
+//     folded into an int64 running sum S = sum_a round(2^24 D_a) held in the
+//     epilogue's registers (exact but for D4's rounding; below 2^60 for a fused
+//     K up to 2^20).  A single fp32 accumulator for the lower groups is not
 //     enough: the tensor core's fp32 accumulation truncates, which loses about
-//     K ulps of the g = 2 terms.)
+//     K ulps of the group it holds.
 //   * C = S * 2^(e_r + f_c - 40), converted to FP64 with integer operations.
 // No FP64 arithmetic runs in the GEMM: GB300 issues about 2 FP64 FMAs per SM
 // per clock against ~4000 bf16 FMAs, so FP64 work stays in the row-exponent
@@ -42,7 +43,9 @@ namespace tq {
 
 constexpr int OZ_THREADS = 320;  // warp 0: loads, warp 1: MMA, warps 2-9: epilogue
 constexpr uint32_t OZ_TMEM_COLS = 512;
-// TMEM columns: accumulator D_a (a = 0..3) at [a*OZ_N, (a+1)*OZ_N)
+// TMEM columns: accumulator D_a (a = 0..4) at [a*OZ_N, (a+1)*OZ_N), 480 of 512
+constexpr int OZ_NACC = 5;
+static_assert(OZ_NACC * OZ_N <= (int)OZ_TMEM_COLS, "accumulators exceed TMEM");
 constexpr int OZ_SMEM_BYTES = 200 * 1024;
 
 __device__ __forceinline__ int64_t oz_find(const int64_t *start, int64_t n, int64_t t) {
@@ -312,7 +315,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
         oz_decode(J, t, T);
         const uint32_t idesc = idesc_bf16_f32(OZ_M, (uint32_t)T.nmma);
         int kc = 0;
-        uint32_t fresh = 0xf;  // bit a: accumulator D_a not yet written in this chunk
+        uint32_t fresh = 0x1f;  // bit a: accumulator D_a not yet written in this chunk
         for (int64_t sidx = T.seg0; sidx < T.seg1 && !abort_flag; sidx++) {
           const int64_t p = J.g.perm ? J.g.perm[sidx] : sidx;
           const int64_t nk = J.nk_pair[p];
@@ -331,7 +334,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
                 break;
               }
               tc_fence_after();
-              fresh = 0xf;
+              fresh = 0x1f;
             }
             const uint32_t sa = smem_u32(smem + st * stage_bytes);
             const uint32_t sb = sa + a_bytes_max;
@@ -339,7 +342,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
               const uint64_t da = smem_desc(sa + ta * T.ga * 256, 128, 256);
               for (int ub = 0; ub < s - ta; ub++) {
                 const uint64_t db = smem_desc(sb + ub * T.gb * 256, 128, 256);
-                const int acc = ta + ub < 3 ? ta + ub : 3;
+                const int acc = ta + ub < OZ_NACC - 1 ? ta + ub : OZ_NACC - 1;
                 mma_bf16(tmem + acc * OZ_N, da, db, idesc, (fresh >> acc) & 1 ? 0u : 1u);
                 fresh &= ~(1u << acc);
               }
@@ -368,7 +371,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
     const int row = 32 * q4 + lane;
     const uint32_t lane_addr = tmem + ((uint32_t)(32 * q4) << 16);
     const int cbase = half * (OZ_N / 2);
-    const int n_acc = s < 4 ? s : 4;  // accumulators the slice products reach
+    const int n_acc = s < OZ_NACC ? s : OZ_NACC;  // accumulators the slice products reach
     uint32_t f = 0;
     for (int64_t t = blockIdx.x; t < J.n_tiles && !abort_flag; t += gridDim.x) {
       OzTile T;
@@ -388,11 +391,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
           break;
         }
         tc_fence_after();
-        // D0..D2 hold whole multiples of 2^-24 below 2^24 (exact); D3 is rounded
+        // 2^24 D_a is a whole number below 2^48 for a <= 3 (exact); D4 is rounded
 #pragma unroll
         for (int x = 0; x < OZ_N / 32; x++) {
 #pragma unroll
-          for (int a = 0; a < 4; a++) {
+          for (int a = 0; a < OZ_NACC; a++) {
             if (a >= n_acc) break;
             uint32_t v[16];
             tmem_ld16(lane_addr + a * OZ_N + cbase + 16 * x, v);
@@ -437,20 +440,25 @@ int oz_stages(int s) {
   return n > OZ_MAX_STAGES ? OZ_MAX_STAGES : n;
 }
 
-tq_status launch_ozaki(const OzJob &job, const OzSide &SA, const OzSide &SB, int64_t rowsA,
-                       int64_t rowsB, int64_t tilesA, int64_t tilesB, int32_t *expA,
-                       int32_t *expB, int64_t nexpA, int64_t nexpB, cudaStream_t st) {
+tq_status launch_ozaki_prepare(const OzJob &job, const OzSide &SA, const OzSide &SB,
+                               int64_t rowsA, int64_t rowsB, int64_t tilesA, int64_t tilesB,
+                               int32_t *expA, int32_t *expB, int64_t nexpA, int64_t nexpB,
+                               cudaStream_t st) {
   const int T = 256;
-  if (nexpA) oz_exp_init_kernel<<<(unsigned)((nexpA + T - 1) / T), T, 0, st>>>(expA, nexpA);
-  if (nexpB) oz_exp_init_kernel<<<(unsigned)((nexpB + T - 1) / T), T, 0, st>>>(expB, nexpB);
-  if (rowsA) oz_rowexp_kernel<<<(unsigned)((rowsA + T - 1) / T), T, 0, st>>>(SA, rowsA, expA);
-  if (rowsB) oz_rowexp_kernel<<<(unsigned)((rowsB + T - 1) / T), T, 0, st>>>(SB, rowsB, expB);
+  if (nexpA) count_launch(), oz_exp_init_kernel<<<(unsigned)((nexpA + T - 1) / T), T, 0, st>>>(expA, nexpA);
+  if (nexpB) count_launch(), oz_exp_init_kernel<<<(unsigned)((nexpB + T - 1) / T), T, 0, st>>>(expB, nexpB);
+  if (rowsA) count_launch(), oz_rowexp_kernel<<<(unsigned)((rowsA + T - 1) / T), T, 0, st>>>(SA, rowsA, expA);
+  if (rowsB) count_launch(), oz_rowexp_kernel<<<(unsigned)((rowsB + T - 1) / T), T, 0, st>>>(SB, rowsB, expB);
   TQ_CUDA(cudaGetLastError());
-  if (tilesA) oz_slice_kernel<<<(unsigned)tilesA, 256, 0, st>>>(SA, job.s, OZ_M, expA,
+  if (tilesA) count_launch(), oz_slice_kernel<<<(unsigned)tilesA, 256, 0, st>>>(SA, job.s, OZ_M, expA,
                                                                   (uint8_t *)job.sliceA);
-  if (tilesB) oz_slice_kernel<<<(unsigned)tilesB, 256, 0, st>>>(SB, job.s, OZ_N, expB,
+  if (tilesB) count_launch(), oz_slice_kernel<<<(unsigned)tilesB, 256, 0, st>>>(SB, job.s, OZ_N, expB,
                                                                   (uint8_t *)job.sliceB);
   TQ_CUDA(cudaGetLastError());
+  return TQ_OK;
+}
+
+tq_status launch_ozaki_gemm(const OzJob &job, cudaStream_t st) {
   if (job.n_tiles == 0) return TQ_OK;
   static int sms = 0;
   if (!sms) {
@@ -461,7 +469,7 @@ tq_status launch_ozaki(const OzJob &job, const OzSide &SA, const OzSide &SB, int
                                  OZ_SMEM_BYTES));
   }
   const int64_t grid = job.n_tiles < sms ? job.n_tiles : sms;
-  oz_gemm_kernel<<<(unsigned)grid, OZ_THREADS, OZ_SMEM_BYTES, st>>>(job);
+  count_launch(), oz_gemm_kernel<<<(unsigned)grid, OZ_THREADS, OZ_SMEM_BYTES, st>>>(job);
   TQ_CUDA(cudaGetLastError());
   return TQ_OK;
 }

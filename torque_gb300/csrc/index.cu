@@ -76,17 +76,17 @@ tq_status scan_exclusive(const int64_t *in, int64_t *out, int64_t n, int64_t *to
   }
   const int64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
   if (tiles == 1) {
-    scan_tiles<<<1, SCAN_T, 0, s>>>(in, out, n, nullptr, total_dev);
+    count_launch(), scan_tiles<<<1, SCAN_T, 0, s>>>(in, out, n, nullptr, total_dev);
     TQ_CUDA(cudaGetLastError());
     return TQ_OK;
   }
   DevArray<int64_t> sums, offs;
   TQ_CHECK(sums.alloc(tiles, s));
   TQ_CHECK(offs.alloc(tiles, s));
-  scan_tile_sums<<<(unsigned)tiles, SCAN_T, 0, s>>>(in, n, sums.p);
+  count_launch(), scan_tile_sums<<<(unsigned)tiles, SCAN_T, 0, s>>>(in, n, sums.p);
   TQ_CUDA(cudaGetLastError());
   TQ_CHECK(scan_exclusive(sums.p, offs.p, tiles, nullptr, s));
-  scan_tiles<<<(unsigned)tiles, SCAN_T, 0, s>>>(in, out, n, offs.p, total_dev);
+  count_launch(), scan_tiles<<<(unsigned)tiles, SCAN_T, 0, s>>>(in, out, n, offs.p, total_dev);
   TQ_CUDA(cudaGetLastError());
   return TQ_OK;
 }
@@ -170,10 +170,10 @@ tq_status radix_sort_pairs(int64_t *keys, int64_t *vals, int64_t n, int key_bits
   const int passes = (key_bits + 7) / 8;
   for (int p = 0; p < passes; p++) {
     const int shift = 8 * p;
-    radix_hist<<<(unsigned)n_tiles, RS_T, 0, s>>>(ka, n, shift, hist.p, n_tiles);
+    count_launch(), radix_hist<<<(unsigned)n_tiles, RS_T, 0, s>>>(ka, n, shift, hist.p, n_tiles);
     TQ_CUDA(cudaGetLastError());
     TQ_CHECK(scan_exclusive(hist.p, offs.p, 256 * n_tiles, nullptr, s));
-    radix_scatter<<<(unsigned)n_tiles, RS_T, 0, s>>>(ka, va, n, shift, offs.p, n_tiles, kb, vb);
+    count_launch(), radix_scatter<<<(unsigned)n_tiles, RS_T, 0, s>>>(ka, va, n, shift, offs.p, n_tiles, kb, vb);
     TQ_CUDA(cudaGetLastError());
     std::swap(ka, kb);
     std::swap(va, vb);
@@ -249,7 +249,7 @@ static tq_status gather(const DevBS &B, const LegSpec &legs, IntervalCache &c, c
   TQ_CHECK(c.lo.alloc((size_t)legs.nc * B.nb, s));
   TQ_CHECK(c.hi.alloc((size_t)legs.nc * B.nb, s));
   if (B.nb) {
-    gather_intervals<<<(unsigned)((B.nb + 255) / 256), 256, 0, s>>>(B, legs, c.lo.p, c.hi.p);
+    count_launch(), gather_intervals<<<(unsigned)((B.nb + 255) / 256), 256, 0, s>>>(B, legs, c.lo.p, c.hi.p);
     TQ_CUDA(cudaGetLastError());
   }
   return TQ_OK;
@@ -261,7 +261,7 @@ tq_status match_pairs(const DevBS &A, const DevBS &B, const LegSpec &legs, int64
   IntervalCache c;
   TQ_CHECK(gather(B, legs, c, s));
   const int64_t threads = A.nb * 32;
-  match_kernel<false><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+  count_launch(), match_kernel<false><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
       A, B.nb, legs, c.lo.p, c.hi.p, counts, nullptr, nullptr, nullptr);
   TQ_CUDA(cudaGetLastError());
   return TQ_OK;
@@ -273,7 +273,7 @@ tq_status emit_pairs(const DevBS &A, const DevBS &B, const LegSpec &legs, const 
   IntervalCache c;
   TQ_CHECK(gather(B, legs, c, s));
   const int64_t threads = A.nb * 32;
-  match_kernel<true><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+  count_launch(), match_kernel<true><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
       A, B.nb, legs, c.lo.p, c.hi.p, nullptr, row_off, pa, pb);
   TQ_CUDA(cudaGetLastError());
   return TQ_OK;

@@ -6,7 +6,7 @@ namespace tq {
 
 constexpr int OZ_M = 128;        // output rows per tile (A side, TMEM lanes)
 constexpr int OZ_N = 96;         // output columns per tile (B side)
-constexpr int OZ_CHUNK = 20;     // k-steps of 16 per exact flush (K = 320)
+constexpr int OZ_CHUNK = 15;     // k-steps of 16 per exact flush (K = 240)
 constexpr int OZ_MAXS = 7;       // most slices supported
 constexpr int OZ_MAX_STAGES = 8;
 constexpr int OZ_EXP_ZERO = -(1 << 20);  // exponent of an all-zero row
@@ -41,8 +41,12 @@ struct OzJob {
 };
 
 int oz_stages(int s);
-tq_status launch_ozaki(const OzJob &job, const OzSide &SA, const OzSide &SB, int64_t rowsA,
-                       int64_t rowsB, int64_t tilesA, int64_t tilesB, int32_t *expA,
-                       int32_t *expB, int64_t nexpA, int64_t nexpB, cudaStream_t st);
+// Row exponents and slices of both operands.
+tq_status launch_ozaki_prepare(const OzJob &job, const OzSide &SA, const OzSide &SB,
+                               int64_t rowsA, int64_t rowsB, int64_t tilesA, int64_t tilesB,
+                               int32_t *expA, int32_t *expB, int64_t nexpA, int64_t nexpB,
+                               cudaStream_t st);
+// The persistent tensor-core GEMM over all output tiles.
+tq_status launch_ozaki_gemm(const OzJob &job, cudaStream_t st);
 
 }  // namespace tq

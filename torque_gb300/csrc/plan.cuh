@@ -30,6 +30,13 @@ struct tq_plan {
   tq::DevArray<int32_t> expA, expB, nk_pair, err;
   tq::DevArray<uint8_t> sliceA, sliceB;
   int64_t rowsA = 0, rowsB = 0, tilesA = 0, tilesB = 0, nexpA = 0, nexpB = 0, tc_tiles = 0;
+  // optional phase timing (events on the launching stream)
+  bool profile = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  ~tq_plan() {
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+  }
 };
 
 namespace tq {

@@ -11,6 +11,9 @@ namespace tq {
 
 static thread_local std::string g_last_error;
 static std::atomic<int64_t> g_alloc_budget{-1};
+static std::atomic<int64_t> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void set_error(const std::string &msg) { g_last_error = msg; }
 
@@ -152,6 +155,8 @@ extern "C" {
 const char *tq_last_error_string(void) { return g_last_error.c_str(); }
 
 void tq_debug_fail_alloc_after(int64_t after) { g_alloc_budget.store(after); }
+
+int64_t tq_debug_kernel_launches(void) { return g_launches.load(); }
 
 tq_status tq_bs_create_empty(tq_dtype dtype, int32_t rank, const int64_t *dimension,
                              tq_bs **out) {

@@ -78,6 +78,10 @@ struct DevArray {
 
 size_t dtype_size(tq_dtype t);
 
+// Every kernel launch of the library goes through this counter (reported by
+// tq_debug_kernel_launches).
+void count_launch();
+
 // ---------------------------------------------------------------- kernels' views
 struct DevBS {
   int32_t rank;

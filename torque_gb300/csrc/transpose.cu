@@ -174,7 +174,7 @@ extern "C" tq_status tq_bs_hard_transpose(const tq_bs *t, const int64_t *perm, t
     TQ_CHECK(tile_start.alloc(t->nb, s));
     TQ_CHECK(total.alloc(1, s));
     const DevBS v = t->view();
-    transpose_tiles_kernel<<<(unsigned)((t->nb + 255) / 256), 256, 0, s>>>(v, (int32_t)perm[0],
+    count_launch(), transpose_tiles_kernel<<<(unsigned)((t->nb + 255) / 256), 256, 0, s>>>(v, (int32_t)perm[0],
                                                                          tiles.p);
     TQ_CHECK(scan_exclusive(tiles.p, tile_start.p, t->nb, total.p, s));
     int64_t n_tiles = 0;
@@ -191,9 +191,9 @@ extern "C" tq_status tq_bs_hard_transpose(const tq_bs *t, const int64_t *perm, t
     if (n_tiles > 0x7fffffffLL) return fail(TQ_ERR_UNSUPPORTED, "more than 2^31 transpose tiles");
     if (n_tiles) {
       if (t->dtype == TQ_F64)
-        transpose_kernel<double><<<(unsigned)n_tiles, 256, 0, s>>>(job);
+        count_launch(), transpose_kernel<double><<<(unsigned)n_tiles, 256, 0, s>>>(job);
       else
-        transpose_kernel<float><<<(unsigned)n_tiles, 256, 0, s>>>(job);
+        count_launch(), transpose_kernel<float><<<(unsigned)n_tiles, 256, 0, s>>>(job);
       TQ_CUDA(cudaGetLastError());
     }
   }
