@@ -380,7 +380,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
       const int64_t grow = T.mt * OZ_M + row;
       const bool row_ok = grow < T.m;
       const int er = row_ok ? J.expA[J.rowA[J.keyA[T.i0]] + grow] : 0;
-      // S: running sum in units of 2^-24 of the leading slice product, exact
+      // S: running sum in units of 2^-u of the leading slice product.  With
+      // u <= 48 - log2(K) the sum stays below 2^62.1 for any data, and u >= 24
+      // keeps D0..D3 (whole multiples of 2^-24) exact.
+      int kb = 0;
+      while (kb < 40 && (int64_t(1) << kb) < 16 * T.ksum) kb++;
+      const int u = 48 - kb < 32 ? 48 - kb : 32;
+      const float unit = __int_as_float((127 + u) << 23);
       long long S[OZ_N / 2];
 #pragma unroll
       for (int y = 0; y < OZ_N / 2; y++) S[y] = 0;
@@ -391,18 +397,20 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
           break;
         }
         tc_fence_after();
-        // 2^24 D_a is a whole number below 2^48 for a <= 3 (exact); D4 is rounded
+        // one 8-column chunk of every accumulator per round, a single wait
 #pragma unroll
-        for (int x = 0; x < OZ_N / 32; x++) {
+        for (int x = 0; x < OZ_N / 16; x++) {
+          uint32_t v[OZ_NACC][8];
+#pragma unroll
+          for (int a = 0; a < OZ_NACC; a++)
+            if (a < n_acc) tmem_ld8(lane_addr + a * OZ_N + cbase + 8 * x, v[a]);
+          tmem_ld_wait();
 #pragma unroll
           for (int a = 0; a < OZ_NACC; a++) {
             if (a >= n_acc) break;
-            uint32_t v[16];
-            tmem_ld16(lane_addr + a * OZ_N + cbase + 16 * x, v);
-            tmem_ld_wait();
 #pragma unroll
-            for (int y = 0; y < 16; y++)
-              S[16 * x + y] += __float2ll_rn(__uint_as_float(v[y]) * 16777216.0f);
+            for (int y = 0; y < 8; y++)
+              S[8 * x + y] += __float2ll_rn(__uint_as_float(v[a][y]) * unit);
           }
         }
         tc_fence_before();
@@ -410,7 +418,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
         if (lane == 0) mbar_arrive(&acc_empty);
       }
       if (abort_flag) break;
-      // C = S * 2^(e_r + f_c - 40)
+      // C = S * 2^(e_r + f_c - 16 - u)
       double *C = (double *)J.g.C + J.g.c_off[T.o];
       const int64_t *rowB = J.rowB + J.keyB[T.j0];
       if (row_ok) {
@@ -419,7 +427,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
           const int64_t gcol = T.nt * OZ_N + cbase + y;
           if (gcol < T.n) {
             const int fc = J.expB[*rowB + gcol];
-            C[grow + gcol * T.m] = oz_i64_ldexp(S[y], er + fc - 40);
+            C[grow + gcol * T.m] = oz_i64_ldexp(S[y], er + fc - 16 - u);
           }
         }
       }
