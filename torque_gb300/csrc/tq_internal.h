@@ -15,7 +15,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/torque_gb300.h"
+#include "torque_gb300.h"
 
 #define TQ_MAXR 12  // maximum rank handled on device (the reference uses 10)
 
