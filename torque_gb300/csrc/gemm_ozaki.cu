@@ -218,6 +218,50 @@ __device__ __forceinline__ double oz_i64_ldexp(long long T, int e) {
 }
 
 // ---------------------------------------------------------------- the GEMM
+// All slice products of one k-step, fully unrolled: product (t, u) goes to
+// accumulator min(t+u, OZ_NACC-1).  Descriptors advance by whole row groups
+// (the start-address field counts 16-byte units).  On the first k-step of a
+// flush chunk the first product into each accumulator overwrites it.
+template <int S>
+__device__ __forceinline__ void oz_issue(uint32_t tmem, uint64_t da0, uint64_t db0,
+                                         uint32_t a_step, uint32_t b_step, uint32_t idesc,
+                                         bool chunk_start) {
+#pragma unroll
+  for (int t = 0; t < S; t++) {
+#pragma unroll
+    for (int u = 0; u < S - t; u++) {
+      const int acc = t + u < OZ_NACC - 1 ? t + u : OZ_NACC - 1;
+      // first (t, u) in this order that lands in accumulator acc
+      const bool first = acc < OZ_NACC - 1 ? t == 0 : (t == 0 && u == OZ_NACC - 1);
+      mma_bf16(tmem + acc * OZ_N, da0 + (uint64_t)(t * a_step), db0 + (uint64_t)(u * b_step),
+               idesc, (chunk_start && first) ? 0u : 1u);
+    }
+  }
+}
+
+__device__ __forceinline__ void oz_issue_s(int s, uint32_t tmem, uint64_t da0, uint64_t db0,
+                                           uint32_t a_step, uint32_t b_step, uint32_t idesc,
+                                           bool chunk_start) {
+  switch (s) {
+    case 1: oz_issue<1>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
+    case 2: oz_issue<2>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
+    case 3: oz_issue<3>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
+    case 4: oz_issue<4>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
+    case 5: oz_issue<5>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
+    case 6: oz_issue<6>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
+    default: oz_issue<7>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
+  }
+}
+
+// Exact fp32 -> int32 for values whose scaled magnitude is below 2^22 (one FMA
+// against 1.5 * 2^23, whose ulp is 1, then an integer subtract; rounds to
+// nearest even like rint); larger values take the conversion unit.
+__device__ __forceinline__ int oz_to_int(float x, float scale) {
+  const float y = x * scale;
+  if (fabsf(y) < 4194304.0f) return __float_as_int(y + 12582912.0f) - 0x4B400000;
+  return __float2int_rn(y);
+}
+
 struct OzTile {
   int64_t o, mt, nt, m, n, i0, j0, seg0, seg1, ksum;
   int32_t ga, gb, nmma;
@@ -315,7 +359,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
         oz_decode(J, t, T);
         const uint32_t idesc = idesc_bf16_f32(OZ_M, (uint32_t)T.nmma);
         int kc = 0;
-        uint32_t fresh = 0x1f;  // bit a: accumulator D_a not yet written in this chunk
         for (int64_t sidx = T.seg0; sidx < T.seg1 && !abort_flag; sidx++) {
           const int64_t p = J.g.perm ? J.g.perm[sidx] : sidx;
           const int64_t nk = J.nk_pair[p];
@@ -334,19 +377,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
                 break;
               }
               tc_fence_after();
-              fresh = 0x1f;
             }
             const uint32_t sa = smem_u32(smem + st * stage_bytes);
-            const uint32_t sb = sa + a_bytes_max;
-            for (int ta = 0; ta < s; ta++) {
-              const uint64_t da = smem_desc(sa + ta * T.ga * 256, 128, 256);
-              for (int ub = 0; ub < s - ta; ub++) {
-                const uint64_t db = smem_desc(sb + ub * T.gb * 256, 128, 256);
-                const int acc = ta + ub < OZ_NACC - 1 ? ta + ub : OZ_NACC - 1;
-                mma_bf16(tmem + acc * OZ_N, da, db, idesc, (fresh >> acc) & 1 ? 0u : 1u);
-                fresh &= ~(1u << acc);
-              }
-            }
+            oz_issue_s(s, tmem, smem_desc(sa, 128, 256), smem_desc(sa + a_bytes_max, 128, 256),
+                       (uint32_t)T.ga * 16, (uint32_t)T.gb * 16, idesc, kc == 0);
             mma_commit(&empty_bar[st]);
             if (++kc == OZ_CHUNK) {
               mma_commit(&acc_full);
@@ -386,7 +420,17 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
       int kb = 0;
       while (kb < 40 && (int64_t(1) << kb) < 16 * T.ksum) kb++;
       const int u = 48 - kb < 32 ? 48 - kb : 32;
-      const float unit = __int_as_float((127 + u) << 23);
+      // D_a (a < 4) holds multiples of 2^-8a below 2^24 * 2^-8a: D_a 2^8a is a
+      // whole number of int32; D4 is rounded at 2^-u
+      float scale[OZ_NACC];
+      int shift[OZ_NACC];
+#pragma unroll
+      for (int a = 0; a < OZ_NACC - 1; a++) {
+        scale[a] = __int_as_float((127 + 8 * a) << 23);
+        shift[a] = u - 8 * a;
+      }
+      scale[OZ_NACC - 1] = __int_as_float((127 + u) << 23);
+      shift[OZ_NACC - 1] = 0;
       long long S[OZ_N / 2];
 #pragma unroll
       for (int y = 0; y < OZ_N / 2; y++) S[y] = 0;
@@ -410,7 +454,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
             if (a >= n_acc) break;
 #pragma unroll
             for (int y = 0; y < 8; y++)
-              S[8 * x + y] += __float2ll_rn(__uint_as_float(v[a][y]) * unit);
+              S[8 * x + y] += (long long)oz_to_int(__uint_as_float(v[a][y]), scale[a]) << shift[a];
           }
         }
         tc_fence_before();
