@@ -151,6 +151,13 @@ tq_status tq_bs_hard_transpose(const tq_bs *t, const int64_t *perm, tq_stream st
 tq_status tq_bs_slice(const tq_bs *t, const int64_t *divisor, tq_stream stream,
                       tq_bs **out);
 
+/* torque::util::nest_sum (src/util/space.h:77-88) on the device: offsets[i] =
+ * counts[0] + ... + counts[i-1], *total = the sum of all n counts.  The block
+ * offsets of a block list are the nest_sum of its block element counts.  All
+ * three pointers are device memory; ordered on stream. */
+tq_status tq_nest_sum(const int64_t *counts, int64_t n, int64_t *offsets, int64_t *total,
+                      tq_stream stream);
+
 /* ---- plans: the symbolic and numeric stages of contract, separately ------- */
 
 typedef struct tq_plan tq_plan;

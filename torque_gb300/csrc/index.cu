@@ -280,3 +280,11 @@ tq_status emit_pairs(const DevBS &A, const DevBS &B, const LegSpec &legs, const 
 }
 
 }  // namespace tq
+
+extern "C" tq_status tq_nest_sum(const int64_t *counts, int64_t n, int64_t *offsets,
+                                 int64_t *total, tq_stream stream) {
+  if (n < 0) return tq::fail(TQ_ERR_INVALID, "negative length");
+  if ((n > 0 && (!counts || !offsets)) || !total)
+    return tq::fail(TQ_ERR_INVALID, "NULL argument");
+  return tq::scan_exclusive(counts, offsets, n, total, (cudaStream_t)stream);
+}
