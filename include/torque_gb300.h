@@ -158,6 +158,17 @@ tq_status tq_bs_slice(const tq_bs *t, const int64_t *divisor, tq_stream stream,
 tq_status tq_nest_sum(const int64_t *counts, int64_t n, int64_t *offsets, int64_t *total,
                       tq_stream stream);
 
+/* tq_nest_sum for callers that cannot allocate device memory (no counterpart in
+ * the reference).  It calls no cudaMalloc/cudaFree and no allocating library
+ * routine: its scratch is a 32 KB array of static device memory that the library
+ * keeps on every GPU that loads it.  At most 4,194,304 counts (larger n returns
+ * TQ_ERR_INVALID).  The first call on a device looks up that array's device
+ * address, so make that first call before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race; sequential calls are
+ * independent. */
+tq_status tq_nest_sum_noalloc(const int64_t *counts, int64_t n, int64_t *offsets,
+                              int64_t *total, tq_stream stream);
+
 /* ---- plans: the symbolic and numeric stages of contract, separately ------- */
 
 typedef struct tq_plan tq_plan;

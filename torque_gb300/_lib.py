@@ -47,6 +47,7 @@ SIGNATURES = {
     "tq_bs_hard_transpose": (ST, [P, P64, P, PP]),
     "tq_bs_slice": (ST, [P, P64, P, PP]),
     "tq_nest_sum": (ST, [P, I64, P, P, P]),
+    "tq_nest_sum_noalloc": (ST, [P, I64, P, P, P]),
     "tq_plan_create": (ST, [P, P, I32, P64, P64, ctypes.POINTER(ContractOpts), P, PP, PP]),
     "tq_plan_execute": (ST, [P, P]),
     "tq_plan_flops": (ST, [P, ctypes.POINTER(ctypes.c_double), P64]),

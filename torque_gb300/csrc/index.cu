@@ -1,6 +1,8 @@
 // Integer index kernels: prefix scans, a stable radix sort and block-pair
 // matching.  Integer work only; every result is bit-exact and independent of
 // scheduling (no atomics decide an order).
+#include <mutex>
+
 #include "index.cuh"
 
 namespace tq {
@@ -287,4 +289,74 @@ extern "C" tq_status tq_nest_sum(const int64_t *counts, int64_t n, int64_t *offs
   if ((n > 0 && (!counts || !offsets)) || !total)
     return tq::fail(TQ_ERR_INVALID, "NULL argument");
   return tq::scan_exclusive(counts, offsets, n, total, (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------- nest_sum without allocation
+// Some callers cannot call cudaMalloc: code that owns all device memory through
+// a fixed arena reserved at start-up, and latency-critical loops in which an
+// allocation may block or synchronise the device.  tq_nest_sum_noalloc serves
+// them: the same three-phase scan as tq_nest_sum, its tile sums and tile
+// offsets kept in the file-scope array below instead of allocated scratch.
+// Limit: TQ_NOALLOC_MAX_TILES tiles of SCAN_TILE counts, i.e. 4,194,304 counts.
+// Every GPU that loads this library holds the 32 KB array until the process
+// exits; every call shares it, so calls that overlap on the GPU race.  Each call
+// writes every scratch entry it reads before reading it, so nothing has to be
+// cleared between calls.
+namespace tq {
+
+constexpr int64_t TQ_NOALLOC_MAX_TILES = 2048;
+constexpr int64_t TQ_NOALLOC_MAX_N = TQ_NOALLOC_MAX_TILES * SCAN_TILE;
+
+static __device__ __align__(256) int64_t g_noalloc_scan[2 * TQ_NOALLOC_MAX_TILES];
+
+// Device address of g_noalloc_scan, looked up once per device with that device
+// current (in host code the symbol itself is only a host-side stand-in).
+static std::mutex g_noalloc_mu;
+static int64_t *g_noalloc_addr[128] = {nullptr};
+
+static tq_status noalloc_scratch(int64_t **out) {
+  int dev = 0;
+  TQ_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return fail(TQ_ERR_UNSUPPORTED, "device ordinal above 127");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scan);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scan)");
+    g_noalloc_addr[dev] = (int64_t *)p;
+  }
+  *out = g_noalloc_addr[dev];
+  return TQ_OK;
+}
+
+}  // namespace tq
+
+extern "C" tq_status tq_nest_sum_noalloc(const int64_t *counts, int64_t n, int64_t *offsets,
+                                         int64_t *total, tq_stream stream) {
+  using namespace tq;
+  if (n < 0) return fail(TQ_ERR_INVALID, "negative length");
+  if ((n > 0 && (!counts || !offsets)) || !total)
+    return fail(TQ_ERR_INVALID, "NULL argument");
+  if (n > TQ_NOALLOC_MAX_N)
+    return fail(TQ_ERR_INVALID, "tq_nest_sum_noalloc takes at most 4194304 counts (got " +
+                                    std::to_string(n) + "); use tq_nest_sum");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (n == 0) {
+    TQ_CUDA(cudaMemsetAsync(total, 0, 8, s));
+    return TQ_OK;
+  }
+  const int64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+  if (tiles == 1) {
+    count_launch(), scan_tiles<<<1, SCAN_T, 0, s>>>(counts, offsets, n, nullptr, total);
+    TQ_CUDA(cudaGetLastError());
+    return TQ_OK;
+  }
+  int64_t *scratch = nullptr;
+  TQ_CHECK(noalloc_scratch(&scratch));
+  int64_t *sums = scratch, *offs = scratch + TQ_NOALLOC_MAX_TILES;
+  count_launch(), scan_tile_sums<<<(unsigned)tiles, SCAN_T, 0, s>>>(counts, n, sums);
+  count_launch(), scan_tiles<<<1, SCAN_T, 0, s>>>(sums, offs, tiles, nullptr, nullptr);
+  count_launch(), scan_tiles<<<(unsigned)tiles, SCAN_T, 0, s>>>(counts, offsets, n, offs, total);
+  TQ_CUDA(cudaGetLastError());
+  return TQ_OK;
 }
