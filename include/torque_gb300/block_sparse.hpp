@@ -1,0 +1,275 @@
+// torque::gpu::BlockSparseTensor<T> over the C ABI of libtorque_gb300.
+//
+// Source-compatible with the reference class (src/gpu/block_sparse.cuh:143-1181):
+// the same constructors, public metadata members, element access, contract,
+// hard_transpose and slice, with T in {float, double}.  Differences:
+//   * contract() takes any handle type in the first position and ignores it (no
+//     cuBLAS is used); an overload without a handle is added;
+//   * API misuse throws Error (as the reference does); CUDA failures throw
+//     std::runtime_error instead of exiting the process;
+//   * contract() accepts a tq_contract_opts for the tensor-core forms and the
+//     reduced layout.
+// The public members are refreshed from the library after every call that
+// changes the block list.
+#pragma once
+
+#if __has_include(<armadillo>) && !defined(TORQUE_GB300_NO_ARMADILLO)
+#include <armadillo>
+#else
+#include "arma_min.hpp"
+#endif
+
+#include <cuda_runtime_api.h>
+
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "../torque_gb300.h"
+
+#ifndef TORQUE_ERROR_H
+struct Error : public std::runtime_error {
+  explicit Error(const std::string &error_message)
+      : std::runtime_error("Error: " + error_message) {}
+  explicit Error(const char *error_message)
+      : std::runtime_error("Error: " + std::string(error_message)) {}
+};
+#endif
+
+namespace torque {
+namespace gpu {
+
+namespace detail {
+inline void check(tq_status st) {
+  if (st == TQ_OK) return;
+  const std::string msg = tq_last_error_string();
+  if (st == TQ_ERR_INVALID || st == TQ_ERR_RANGE || st == TQ_ERR_UNSUPPORTED) throw Error(msg);
+  throw std::runtime_error("torque_gb300: " + msg);
+}
+
+inline std::vector<int64_t> flat(const arma::uvec &v) {
+  std::vector<int64_t> out(v.n_elem);
+  for (arma::uword i = 0; i < v.n_elem; i++) out[i] = (int64_t)v(i);
+  return out;
+}
+
+// rank x n matrix (column = block) -> the same memory as int64
+inline std::vector<int64_t> flat(const arma::umat &m) {
+  std::vector<int64_t> out(m.n_elem);
+  for (arma::uword c = 0; c < m.n_cols; c++)
+    for (arma::uword r = 0; r < m.n_rows; r++) out[c * m.n_rows + r] = (int64_t)m(r, c);
+  return out;
+}
+
+template <typename T>
+constexpr tq_dtype dtype() {
+  static_assert(std::is_same<T, float>::value || std::is_same<T, double>::value,
+                "torque_gb300 supports float and double tensors");
+  return std::is_same<T, float>::value ? TQ_F32 : TQ_F64;
+}
+
+inline tq_memkind kind_of(cudaMemcpyKind k) {
+  return (k == cudaMemcpyHostToDevice || k == cudaMemcpyHostToHost) ? TQ_MEM_HOST : TQ_MEM_DEVICE;
+}
+}  // namespace detail
+
+template <typename T>
+class BlockSparseTensor {
+ public:
+  arma::uword rank = 0;
+  arma::uvec dimension;
+  arma::umat blocks_dimension;
+  arma::umat index_tables;
+  arma::umat begin_points;
+  arma::umat end_points;
+  arma::uvec block_n_elem;
+  arma::uvec block_offsets;
+
+  explicit BlockSparseTensor(const arma::uvec &dim) {
+    const auto d = detail::flat(dim);
+    detail::check(tq_bs_create_empty(detail::dtype<T>(), (int32_t)dim.n_elem, d.data(), &h_));
+    refresh();
+  }
+
+  BlockSparseTensor(const T *source_data, const arma::umat &begin, const arma::umat &end,
+                    const arma::uvec &total_dimension,
+                    const cudaMemcpyKind kind = cudaMemcpyHostToDevice) {
+    create(source_data, begin, end, total_dimension, nullptr, kind);
+  }
+
+  BlockSparseTensor(const T *source_data, const arma::umat &begin, const arma::umat &end,
+                    const arma::uvec &total_dimension, const arma::umat &tables,
+                    const cudaMemcpyKind kind = cudaMemcpyDeviceToDevice) {
+    create(source_data, begin, end, total_dimension, &tables, kind);
+  }
+
+  BlockSparseTensor(const BlockSparseTensor &o) {
+    detail::check(tq_bs_clone(o.h_, nullptr, &h_));
+    refresh();
+  }
+  BlockSparseTensor(BlockSparseTensor &&o) noexcept { swap(*this, o); }
+  BlockSparseTensor &operator=(BlockSparseTensor &&o) noexcept {
+    swap(*this, o);
+    return *this;
+  }
+  BlockSparseTensor &operator=(const BlockSparseTensor &o) {
+    BlockSparseTensor tmp(o);
+    swap(*this, tmp);
+    return *this;
+  }
+  ~BlockSparseTensor() {
+    if (h_) tq_bs_destroy(h_);
+  }
+
+  friend void swap(BlockSparseTensor &a, BlockSparseTensor &b) noexcept {
+    std::swap(a.h_, b.h_);
+    std::swap(a.rank, b.rank);
+    std::swap(a.dimension, b.dimension);
+    std::swap(a.blocks_dimension, b.blocks_dimension);
+    std::swap(a.index_tables, b.index_tables);
+    std::swap(a.begin_points, b.begin_points);
+    std::swap(a.end_points, b.end_points);
+    std::swap(a.block_n_elem, b.block_n_elem);
+    std::swap(a.block_offsets, b.block_offsets);
+  }
+
+  T to_number() const {
+    T v;
+    detail::check(tq_bs_to_number(h_, &v));
+    return v;
+  }
+
+  void append_block(const T *source_data, const arma::uvec &begin_point,
+                    const arma::uvec &end_point, const arma::uvec &index_table,
+                    const cudaMemcpyKind kind = cudaMemcpyHostToDevice) {
+    const auto b = detail::flat(begin_point), e = detail::flat(end_point),
+               t = detail::flat(index_table);
+    if (b.size() != rank || e.size() != rank) throw Error("Rank does not match");
+    detail::check(tq_bs_append_blocks(h_, 1, b.data(), e.data(),
+                                      t.size() == rank ? t.data() : nullptr, source_data,
+                                      detail::kind_of(kind), nullptr));
+    refresh();
+  }
+
+  void append_blocks(const T *const source_data, const arma::umat &begin,
+                     const arma::umat &end, const arma::umat &tables,
+                     const cudaMemcpyKind kind = cudaMemcpyHostToDevice) {
+    const auto b = detail::flat(begin), e = detail::flat(end), t = detail::flat(tables);
+    detail::check(tq_bs_append_blocks(h_, (int64_t)begin.n_cols, b.data(), e.data(),
+                                      t.size() == b.size() ? t.data() : nullptr, source_data,
+                                      detail::kind_of(kind), nullptr));
+    refresh();
+  }
+
+  void modify(const arma::uvec &indices, const T number) {
+    if (indices.n_elem != rank) throw Error("Rank does not match");
+    const auto i = detail::flat(indices);
+    detail::check(tq_bs_modify(h_, i.data(), &number));
+    refresh();
+  }
+
+  T query(const arma::uvec &indices) const {
+    if (indices.n_elem != rank) throw Error("Rank does not match");
+    const auto i = detail::flat(indices);
+    T v;
+    detail::check(tq_bs_query(h_, i.data(), &v));
+    return v;
+  }
+
+  // contract(handle, tensor, contracting_indices): the handle is accepted for
+  // source compatibility and not used.
+  template <typename Handle>
+  BlockSparseTensor contract(Handle, const BlockSparseTensor &tensor,
+                             const arma::umat &contracting_indices,
+                             const tq_contract_opts *opts = nullptr) const {
+    return contract(tensor, contracting_indices, opts);
+  }
+
+  BlockSparseTensor contract(const BlockSparseTensor &tensor,
+                             const arma::umat &contracting_indices,
+                             const tq_contract_opts *opts = nullptr) const {
+    if (contracting_indices.n_elem && contracting_indices.n_cols != 2)
+      throw Error("contracting indices must be an n x 2 matrix");
+    const arma::uword n = contracting_indices.n_elem ? contracting_indices.n_rows : 0;
+    std::vector<int64_t> al(n), bl(n);
+    for (arma::uword k = 0; k < n; k++) {
+      al[k] = (int64_t)contracting_indices(k, 0);
+      bl[k] = (int64_t)contracting_indices(k, 1);
+    }
+    tq_bs *out = nullptr;
+    detail::check(tq_bs_contract(h_, tensor.h_, (int32_t)n, al.data(), bl.data(), opts, nullptr,
+                                 &out));
+    return BlockSparseTensor(out);
+  }
+
+  BlockSparseTensor hard_transpose(const arma::uvec &permutation) const {
+    if (permutation.n_elem != rank)
+      throw Error("The number of permutation does not match the rank of tensor");
+    const auto p = detail::flat(permutation);
+    tq_bs *out = nullptr;
+    detail::check(tq_bs_hard_transpose(h_, p.data(), nullptr, &out));
+    return BlockSparseTensor(out);
+  }
+
+  BlockSparseTensor slice(const arma::uvec &divisor) const {
+    const auto d = detail::flat(divisor);
+    tq_bs *out = nullptr;
+    detail::check(tq_bs_slice(h_, d.data(), nullptr, &out));
+    return BlockSparseTensor(out);
+  }
+
+  // the underlying handle, for calls of the C ABI not wrapped here
+  tq_bs *handle() const { return h_; }
+
+ private:
+  explicit BlockSparseTensor(tq_bs *h) : h_(h) { refresh(); }
+
+  void create(const T *src, const arma::umat &begin, const arma::umat &end,
+              const arma::uvec &dim, const arma::umat *tables, cudaMemcpyKind kind) {
+    const auto d = detail::flat(dim), b = detail::flat(begin), e = detail::flat(end);
+    std::vector<int64_t> t;
+    if (tables) t = detail::flat(*tables);
+    const int64_t nb = dim.n_elem ? (int64_t)begin.n_cols : 0;
+    detail::check(tq_bs_create(detail::dtype<T>(), (int32_t)dim.n_elem, d.data(), nb, b.data(),
+                               e.data(), tables ? t.data() : nullptr, src,
+                               detail::kind_of(kind), nullptr, &h_));
+    refresh();
+  }
+
+  void refresh() {
+    tq_dtype dt;
+    int32_t r = 0;
+    int64_t nb = 0, ne = 0;
+    detail::check(tq_bs_shape(h_, &dt, &r, &nb, &ne));
+    std::vector<int64_t> d(r), b(nb * r), e(nb * r), t(nb * r), off(nb);
+    detail::check(tq_bs_metadata(h_, d.data(), b.data(), e.data(), t.data(), off.data()));
+    rank = (arma::uword)r;
+    dimension = arma::uvec(rank);
+    for (int32_t l = 0; l < r; l++) dimension(l) = (arma::uword)d[l];
+    begin_points = arma::umat(rank, nb);
+    end_points = arma::umat(rank, nb);
+    index_tables = arma::umat(rank, nb);
+    blocks_dimension = arma::umat(rank, nb);
+    block_n_elem = arma::uvec(nb);
+    block_offsets = arma::uvec(nb);
+    for (int64_t k = 0; k < nb; k++) {
+      arma::uword cnt = 1;
+      for (int32_t l = 0; l < r; l++) {
+        begin_points(l, k) = (arma::uword)b[k * r + l];
+        end_points(l, k) = (arma::uword)e[k * r + l];
+        index_tables(l, k) = (arma::uword)t[k * r + l];
+        blocks_dimension(l, k) = end_points(l, k) - begin_points(l, k) + 1;
+        cnt *= blocks_dimension(l, k);
+      }
+      block_n_elem(k) = cnt;
+      block_offsets(k) = (arma::uword)off[k];
+    }
+  }
+
+  tq_bs *h_ = nullptr;
+};
+
+}  // namespace gpu
+}  // namespace torque
