@@ -195,6 +195,31 @@ tq_status tq_plan_last_timings(tq_plan *plan, float *prepare_ms, float *gemm_ms)
 tq_status tq_plan_check(tq_plan *plan, tq_stream stream);
 tq_status tq_plan_destroy(tq_plan *plan);
 
+/* ---- batches: many contractions in one launch -------------------------- */
+
+typedef struct tq_batch tq_batch;
+
+/* Groups planned contractions into one numeric stage.  Plans in the same wave
+ * are independent: the operand preparation of all their tensor-core plans runs
+ * as one set of kernels and their block GEMMs as ONE persistent launch over the
+ * output tiles of every plan.  wave[i] (non-decreasing; NULL = all in wave 0)
+ * orders dependent contractions: a wave may read results of earlier waves
+ * (e.g. the two contractions of a PEPS site update).  Native-precision and
+ * rank-0 plans run after the tensor-core launch of their wave.  The plans must
+ * outlive the batch. */
+tq_status tq_batch_create(tq_plan *const *plans, int32_t n, const int32_t *wave,
+                          tq_stream stream, tq_batch **out);
+/* The numeric stage of every plan, ordered on stream; no host synchronisation,
+ * no allocation (capturable). */
+tq_status tq_batch_execute(tq_batch *batch, tq_stream stream);
+/* The same as one CUDA graph: captured on the first call, replayed after. */
+tq_status tq_batch_graph_launch(tq_batch *batch, tq_stream stream);
+/* Bounded-wait status of the last execution (synchronises the stream). */
+tq_status tq_batch_check(tq_batch *batch, tq_stream stream);
+/* Kernels one execution of the batch launches. */
+tq_status tq_batch_kernels(const tq_batch *batch, int64_t *kernels);
+tq_status tq_batch_destroy(tq_batch *batch);
+
 /* ---- errors and hooks -------------------------------------------------- */
 
 /* Message of the last failing call on this thread. */

@@ -5,7 +5,7 @@ include/torque_gb300.h); this package is its Python binding and the host-side
 helpers (charge-sector constructors, synthetic workloads).
 """
 from ._lib import TorqueError, load  # noqa: F401
-from .block_sparse import BlockSparseTensor, ContractionPlan  # noqa: F401
+from .block_sparse import Batch, BlockSparseTensor, ContractionPlan  # noqa: F401
 from .sectors import BlockList, Leg, charge_blocks  # noqa: F401
 
 __all__ = ["BlockSparseTensor", "ContractionPlan", "TorqueError", "Leg", "BlockList",

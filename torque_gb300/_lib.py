@@ -56,6 +56,12 @@ SIGNATURES = {
     "tq_plan_last_timings": (ST, [P, ctypes.POINTER(ctypes.c_float),
                                   ctypes.POINTER(ctypes.c_float)]),
     "tq_plan_check": (ST, [P, P]),
+    "tq_batch_create": (ST, [PP, I32, ctypes.POINTER(I32), P, PP]),
+    "tq_batch_execute": (ST, [P, P]),
+    "tq_batch_graph_launch": (ST, [P, P]),
+    "tq_batch_check": (ST, [P, P]),
+    "tq_batch_kernels": (ST, [P, P64]),
+    "tq_batch_destroy": (ST, [P]),
     "tq_last_error_string": (ctypes.c_char_p, []),
     "tq_debug_fail_alloc_after": (None, [I64]),
     "tq_debug_kernel_launches": (I64, []),

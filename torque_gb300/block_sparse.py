@@ -309,3 +309,43 @@ class ContractionPlan:
             except Exception:
                 pass
             self._p = ctypes.c_void_p()
+
+
+class Batch:
+    """Many planned contractions as one numeric stage (tq_batch_*): the
+    tensor-core plans of each wave share one persistent GEMM launch; the whole
+    batch can be captured once as a CUDA graph and replayed."""
+
+    def __init__(self, plans, waves=None, stream=None):
+        self.plans = list(plans)  # keep the plans (and their tensors) alive
+        n = len(self.plans)
+        arr = (ctypes.c_void_p * max(n, 1))(*[p._p.value for p in self.plans])
+        w = None
+        if waves is not None:
+            w = (ctypes.c_int32 * max(n, 1))(*[int(x) for x in waves])
+        self._b = ctypes.c_void_p()
+        check(load().tq_batch_create(arr, n, w, _stream(stream), ctypes.byref(self._b)))
+
+    def execute(self, stream=None):
+        check(load().tq_batch_execute(self._b, _stream(stream)))
+
+    def graph_launch(self, stream=None):
+        check(load().tq_batch_graph_launch(self._b, _stream(stream)))
+
+    def check(self, stream=None):
+        check(load().tq_batch_check(self._b, _stream(stream)))
+
+    @property
+    def kernels(self) -> int:
+        k = ctypes.c_int64()
+        check(load().tq_batch_kernels(self._b, ctypes.byref(k)))
+        return k.value
+
+    def __del__(self):
+        b = getattr(self, "_b", None)
+        if b is not None and b.value:
+            try:
+                load().tq_batch_destroy(b)
+            except Exception:
+                pass
+            self._b = ctypes.c_void_p()

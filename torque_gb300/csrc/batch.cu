@@ -1,0 +1,140 @@
+// Batches: many planned contractions as one numeric stage (one persistent
+// tensor-core GEMM launch per wave of independent contractions), optionally
+// captured once as a CUDA graph and replayed.
+#include <memory>
+#include <vector>
+
+#include "ozaki.cuh"
+#include "plan.cuh"
+
+namespace tq {
+tq_status plan_run(tq_plan *P, cudaStream_t s);
+tq_status plan_check(tq_plan *P, cudaStream_t s);
+}  // namespace tq
+
+using namespace tq;
+
+struct tq_batch {
+  struct Wave {
+    OzBatchDev oz;                 // the tensor-core plans of the wave, as one launch
+    bool has_oz = false;
+    std::vector<tq_plan *> others;  // native-precision, rank-0 or empty plans
+  };
+  std::vector<std::unique_ptr<Wave>> waves;
+  std::vector<tq_plan *> plans;
+  cudaStream_t capture_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t kernels = 0;
+  ~tq_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (capture_stream) cudaStreamDestroy(capture_stream);
+  }
+};
+
+static tq_status batch_run(tq_batch *b, cudaStream_t s) {
+  for (auto &w : b->waves) {
+    if (w->has_oz) {
+      TQ_CHECK(oz_batch_prepare(w->oz, s));
+      TQ_CHECK(oz_batch_gemm(w->oz, s));
+    }
+    for (tq_plan *P : w->others) TQ_CHECK(plan_run(P, s));
+  }
+  return TQ_OK;
+}
+
+extern "C" {
+
+tq_status tq_batch_create(tq_plan *const *plans, int32_t n, const int32_t *wave, tq_stream stream,
+                          tq_batch **out) {
+  if (!out || (n > 0 && !plans)) return fail(TQ_ERR_INVALID, "NULL argument");
+  if (n < 0) return fail(TQ_ERR_INVALID, "negative plan count");
+  for (int32_t i = 0; i < n; i++) {
+    if (!plans[i]) return fail(TQ_ERR_INVALID, "plan is NULL");
+    if (wave && i && wave[i] < wave[i - 1])
+      return fail(TQ_ERR_INVALID, "waves must be non-decreasing");
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  std::unique_ptr<tq_batch> b(new tq_batch());
+  b->plans.assign(plans, plans + n);
+  int32_t i = 0;
+  while (i < n) {
+    const int32_t wv = wave ? wave[i] : 0;
+    std::unique_ptr<tq_batch::Wave> w(new tq_batch::Wave());
+    std::vector<OzJob> jobs;
+    std::vector<OzSide> sides;
+    for (; i < n && (wave ? wave[i] : 0) == wv; i++) {
+      tq_plan *P = plans[i];
+      if (P->tc && P->C->rank > 0 && P->tc_tiles > 0) {
+        jobs.push_back(P->tc_job);
+        sides.push_back(P->tc_side[0]);
+        sides.push_back(P->tc_side[1]);
+      } else {
+        w->others.push_back(P);
+      }
+    }
+    if (!jobs.empty()) {
+      TQ_CHECK(oz_batch_build(jobs, sides, s, w->oz));
+      w->has_oz = true;
+    }
+    b->waves.push_back(std::move(w));
+  }
+  *out = b.release();
+  return TQ_OK;
+}
+
+tq_status tq_batch_execute(tq_batch *b, tq_stream stream) {
+  if (!b) return fail(TQ_ERR_INVALID, "batch is NULL");
+  const int64_t k0 = tq_debug_kernel_launches();
+  TQ_CHECK(batch_run(b, (cudaStream_t)stream));
+  b->kernels = tq_debug_kernel_launches() - k0;
+  return TQ_OK;
+}
+
+tq_status tq_batch_graph_launch(tq_batch *b, tq_stream stream) {
+  if (!b) return fail(TQ_ERR_INVALID, "batch is NULL");
+  if (!b->exec) {
+    // capture on a private stream (the legacy stream cannot be captured)
+    TQ_CUDA(cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking));
+    TQ_CUDA(cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal));
+    const int64_t k0 = tq_debug_kernel_launches();
+    tq_status st = batch_run(b, b->capture_stream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(b->capture_stream, &g);
+    if (st != TQ_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    TQ_CUDA(e);
+    b->graph = g;
+    b->kernels = tq_debug_kernel_launches() - k0;
+    TQ_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  }
+  TQ_CUDA(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+  return TQ_OK;
+}
+
+tq_status tq_batch_check(tq_batch *b, tq_stream stream) {
+  if (!b) return fail(TQ_ERR_INVALID, "batch is NULL");
+  cudaStream_t s = (cudaStream_t)stream;
+  TQ_CUDA(cudaStreamSynchronize(s));
+  for (auto &w : b->waves) {
+    if (w->has_oz) TQ_CHECK(oz_batch_check(w->oz, s));
+    for (tq_plan *P : w->others) TQ_CHECK(plan_check(P, s));
+  }
+  return TQ_OK;
+}
+
+tq_status tq_batch_kernels(const tq_batch *b, int64_t *kernels) {
+  if (!b || !kernels) return fail(TQ_ERR_INVALID, "NULL argument");
+  *kernels = b->kernels;
+  return TQ_OK;
+}
+
+tq_status tq_batch_destroy(tq_batch *b) {
+  delete b;
+  return TQ_OK;
+}
+
+}  // extern "C"

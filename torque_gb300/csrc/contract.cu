@@ -248,6 +248,22 @@ __global__ void tc_out_kernel(DevBS A, DevBS B, LegSpec L, const int32_t *pa, co
   tiles[o] = ((m + OZ_M - 1) / OZ_M) * ((n + OZ_N - 1) / OZ_N);
 }
 
+GemmJob make_gemm_job(const tq_plan *P) {
+  GemmJob job;
+  job.A = P->A->view();
+  job.B = P->B->view();
+  job.L = P->L;
+  job.pa = P->pa.p;
+  job.pb = P->pb.p;
+  job.seg = P->seg.p;
+  job.perm = P->perm.p;
+  job.tile_start = P->tile_start.p;
+  job.c_off = P->C->d_meta.p ? P->C->d_meta.p + 3 * P->n_out * P->C->rank : nullptr;
+  job.C = P->C->data;
+  job.n_out = P->n_out;
+  return job;
+}
+
 static OzSide make_side(const tq_bs *T, int32_t nfree, const int32_t *fl, int32_t ncon,
                         const int32_t *con, const int64_t *key, const int64_t *row_off,
                         const int64_t *row_start, const int64_t *tile_start,
@@ -345,19 +361,27 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   TQ_CHECK(P->expB.alloc(std::max<int64_t>(P->nexpB, 1), s));
   TQ_CHECK(P->sliceA.alloc(std::max<int64_t>(h[2], 1) * 256, s));
   TQ_CHECK(P->sliceB.alloc(std::max<int64_t>(h[6], 1) * 256, s));
-  TQ_CHECK(P->err.alloc(1, s));
-  TQ_CUDA(cudaMemsetAsync(P->err.p, 0, 4, s));
-  return TQ_OK;
-}
-
-static tq_status run_tc(tq_plan *P, const GemmJob &g, cudaStream_t s) {
-  const LegSpec &L = P->L;
-  OzSide SA = make_side(P->A, L.nfa, L.fa, L.nc, L.al, P->keyA.p, P->rowA.p, P->rowstartA.p,
-                        P->tilestartA.p, P->unitA.p);
-  OzSide SB = make_side(P->B, L.nfb, L.fb, L.nc, L.bl, P->keyB.p, P->rowB.p, P->rowstartB.p,
-                        P->tilestartB.p, P->unitB.p);
-  OzJob J;
-  J.g = g;
+  // this contraction as a batch of one job with two operand sides
+  P->tc_side[0] = make_side(A, L.nfa, L.fa, L.nc, L.al, P->keyA.p, P->rowA.p, P->rowstartA.p,
+                            P->tilestartA.p, P->unitA.p);
+  P->tc_side[1] = make_side(B, L.nfb, L.fb, L.nc, L.bl, P->keyB.p, P->rowB.p, P->rowstartB.p,
+                            P->tilestartB.p, P->unitB.p);
+  const int64_t n_rows[2] = {P->rowsA, P->rowsB}, n_tiles[2] = {P->tilesA, P->tilesB},
+                n_exps[2] = {P->nexpA, P->nexpB};
+  int32_t *exps[2] = {P->expA.p, P->expB.p};
+  uint8_t *slices[2] = {P->sliceA.p, P->sliceB.p};
+  for (int k = 0; k < 2; k++) {
+    OzSide &S = P->tc_side[k];
+    S.exps = exps[k];
+    S.slices = slices[k];
+    S.n_rows = n_rows[k];
+    S.n_tiles = n_tiles[k];
+    S.n_exps = n_exps[k];
+    S.s = sl;
+    S.rt_rows = k == 0 ? OZ_M : OZ_N;
+  }
+  OzJob &J = P->tc_job;
+  J.g = make_gemm_job(P);
   J.tile_start = P->tc_tile_start.p;
   J.n_tiles = P->tc_tiles;
   J.ksum = P->ksum.p;
@@ -372,13 +396,14 @@ static tq_status run_tc(tq_plan *P, const GemmJob &g, cudaStream_t s) {
   J.rowB = P->rowB.p;
   J.expA = P->expA.p;
   J.expB = P->expB.p;
-  J.s = P->slices;
-  J.nstages = oz_stages(P->slices);
-  J.err = P->err.p;
-  TQ_CHECK(launch_ozaki_prepare(J, SA, SB, P->rowsA, P->rowsB, P->tilesA, P->tilesB, P->expA.p,
-                                P->expB.p, P->nexpA, P->nexpB, s));
+  J.s = sl;
+  return oz_batch_build({J}, {P->tc_side[0], P->tc_side[1]}, s, P->tcb);
+}
+
+static tq_status run_tc(tq_plan *P, cudaStream_t s) {
+  TQ_CHECK(oz_batch_prepare(P->tcb, s));
   if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[1], s));
-  return launch_ozaki_gemm(J, s);
+  return oz_batch_gemm(P->tcb, s);
 }
 
 tq_status validate_legs(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,
@@ -561,18 +586,7 @@ tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64
 }
 
 tq_status plan_run(tq_plan *P, cudaStream_t s) {
-  GemmJob job;
-  job.A = P->A->view();
-  job.B = P->B->view();
-  job.L = P->L;
-  job.pa = P->pa.p;
-  job.pb = P->pb.p;
-  job.seg = P->seg.p;
-  job.perm = P->perm.p;
-  job.tile_start = P->tile_start.p;
-  job.c_off = P->C->d_meta.p ? P->C->d_meta.p + 3 * P->n_out * P->C->rank : nullptr;
-  job.C = P->C->data;
-  job.n_out = P->n_out;
+  const GemmJob job = make_gemm_job(P);
   if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[0], s));
   tq_status st = TQ_OK;
   if (P->C->rank == 0) {
@@ -580,7 +594,7 @@ tq_status plan_run(tq_plan *P, cudaStream_t s) {
     st = launch_dot_native(job, P->n_pairs, P->chunk_start.p, P->n_chunks, P->partials.p,
                            P->A->dtype, s);
   } else if (P->tc && P->n_tiles) {
-    st = run_tc(P, job, s);
+    st = run_tc(P, s);
   } else {
     if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[1], s));
     if (P->n_tiles) st = launch_gemm_native(job, P->n_tiles, P->A->dtype, s);
@@ -590,14 +604,8 @@ tq_status plan_run(tq_plan *P, cudaStream_t s) {
 }
 
 tq_status plan_check(tq_plan *P, cudaStream_t s) {
-  if (!P->tc || !P->err.p) return TQ_OK;
-  int32_t e = 0;
-  TQ_CUDA(cudaMemcpyAsync(&e, P->err.p, 4, cudaMemcpyDeviceToHost, s));
-  TQ_CUDA(cudaStreamSynchronize(s));
-  if (e)
-    return fail(TQ_ERR_TIMEOUT,
-                "a tensor-core pipeline wait gave up (flags " + std::to_string(e) + ")");
-  return TQ_OK;
+  if (!P->tc || !P->tcb.err.p) return TQ_OK;
+  return oz_batch_check(P->tcb, s);
 }
 
 }  // namespace tq

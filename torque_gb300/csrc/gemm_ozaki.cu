@@ -64,37 +64,46 @@ __device__ __forceinline__ int64_t free_rows(const DevBS &T, int64_t b, int32_t 
   return m;
 }
 
-// ---------------------------------------------------------------- exponents
-__global__ void oz_exp_init_kernel(int32_t *e, int64_t n) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) e[i] = OZ_EXP_ZERO;
-}
-
-// One thread per (block, row): max |x| over the row's contracted columns.
-__global__ void oz_rowexp_kernel(OzSide S, int64_t total_rows, int32_t *exps) {
-  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= total_rows) return;
-  const int64_t b = oz_find(S.row_start, S.T.nb, g);
-  const int64_t r = g - S.row_start[b];
-  Operand op;
+__device__ __forceinline__ void side_operand(const OzSide &S, int64_t b, Operand &op) {
   int64_t cb[TQ_MAXR], ce[TQ_MAXR];
   for (int k = 0; k < S.ncon; k++) {
     cb[k] = S.T.begin[b * S.T.rank + S.con[k]];
     ce[k] = S.T.end[b * S.T.rank + S.con[k]];
   }
   build_operand(S.T, b, S.nfree, S.free_legs, S.ncon, S.con, cb, ce, op);
+}
+
+// ---------------------------------------------------------------- exponents
+__global__ void oz_exp_init_kernel(OzLaunch L) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= L.n_exps) return;
+  const int64_t k = oz_find(L.side_exp_start, L.n_sides, g);
+  L.sides[k].exps[g - L.side_exp_start[k]] = OZ_EXP_ZERO;
+}
+
+// One thread per (side, block, row): max |x| over the row's contracted columns.
+__global__ void oz_rowexp_kernel(OzLaunch L) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= L.n_rows) return;
+  const int64_t k = oz_find(L.side_row_start, L.n_sides, g);
+  const OzSide &S = L.sides[k];
+  const int64_t lr = g - L.side_row_start[k];
+  const int64_t b = oz_find(S.row_start, S.T.nb, lr);
+  const int64_t r = lr - S.row_start[b];
+  Operand op;
+  side_operand(S, b, op);
   const double *d = (const double *)S.T.data;
   const int64_t ra = op.base + mixed_addr(r, op.nr, op.rdim, op.rst);
   unsigned long long mx = 0;
-  for (int64_t k = 0; k < op.cols; k++) {
+  for (int64_t c = 0; c < op.cols; c++) {
     const unsigned long long bits =
-        (unsigned long long)__double_as_longlong(d[ra + mixed_addr(k, op.nc, op.cdim, op.cst)]) &
+        (unsigned long long)__double_as_longlong(d[ra + mixed_addr(c, op.nc, op.cdim, op.cst)]) &
         0x7fffffffffffffffull;
     mx = bits > mx ? bits : mx;
   }
   if (mx == 0) return;
   const int e = ilogb(__longlong_as_double((long long)mx)) + 2;
-  atomicMax(&exps[S.row_off[S.key[b]] + r], e);
+  atomicMax(&S.exps[S.row_off[S.key[b]] + r], e);
 }
 
 // x * 2^shift rounded to the nearest integer (ties to even), integer ops only.
@@ -123,29 +132,27 @@ __device__ __forceinline__ long long oz_fixed(double x, int shift) {
   return (b >> 63) ? -(long long)q : (long long)q;
 }
 
-// One CTA per (block, row tile): slices of all k-steps of the tile.
-__global__ void __launch_bounds__(256) oz_slice_kernel(OzSide S, int32_t s, int32_t rt_rows,
-                                                       const int32_t *exps, uint8_t *out) {
-  const int64_t tile = blockIdx.x;
-  const int64_t b = oz_find(S.tile_start, S.T.nb, tile);
-  const int64_t rt = tile - S.tile_start[b];
+// One CTA per (side, block, row tile): slices of all k-steps of the tile.
+__global__ void __launch_bounds__(256) oz_slice_kernel(OzLaunch L) {
+  const int64_t g = blockIdx.x;
+  const int64_t k = oz_find(L.side_tile_start, L.n_sides, g);
+  const OzSide &S = L.sides[k];
+  const int64_t lt = g - L.side_tile_start[k];
+  const int64_t b = oz_find(S.tile_start, S.T.nb, lt);
+  const int64_t rt = lt - S.tile_start[b];
+  const int s = S.s, rt_rows = S.rt_rows;
   Operand op;
-  int64_t cb[TQ_MAXR], ce[TQ_MAXR];
-  for (int k = 0; k < S.ncon; k++) {
-    cb[k] = S.T.begin[b * S.T.rank + S.con[k]];
-    ce[k] = S.T.end[b * S.T.rank + S.con[k]];
-  }
-  build_operand(S.T, b, S.nfree, S.free_legs, S.ncon, S.con, cb, ce, op);
+  side_operand(S, b, op);
   const int64_t rows = op.rows - rt * rt_rows < rt_rows ? op.rows - rt * rt_rows : rt_rows;
   const int G = (int)((rows + 7) / 8);
   const int64_t nk = (op.cols + 15) / 16;
-  uint8_t *base = out + 256 * S.unit_off[b] + nk * (int64_t)s * 256 * (rt_rows / 8) * rt;
+  uint8_t *base = S.slices + 256 * S.unit_off[b] + nk * (int64_t)s * 256 * (rt_rows / 8) * rt;
   const double *d = (const double *)S.T.data;
   const int r = threadIdx.x >> 1, c = threadIdx.x & 1;
   if (r >= G * 8) return;
   const int64_t grow = rt * rt_rows + r;
   const bool row_ok = r < rows;
-  const int e = row_ok ? exps[S.row_off[S.key[b]] + grow] : OZ_EXP_ZERO;
+  const int e = row_ok ? S.exps[S.row_off[S.key[b]] + grow] : OZ_EXP_ZERO;
   const int shift = 8 * s - e;
   const int64_t ra = row_ok ? op.base + mixed_addr(grow, op.nr, op.rdim, op.rst) : 0;
   for (int64_t q = 0; q < nk; q++) {
@@ -157,9 +164,9 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OzSide S, int32_t s, int3
       for (int w = 0; w < 4; w++) packed[t][w] = 0;
 #pragma unroll
     for (int x = 0; x < 8; x++) {
-      const int64_t k = q * 16 + c * 8 + x;
+      const int64_t kk = q * 16 + c * 8 + x;
       long long F = 0;
-      if (row_ok && k < op.cols) F = oz_fixed(d[ra + mixed_addr(k, op.nc, op.cdim, op.cst)], shift);
+      if (row_ok && kk < op.cols) F = oz_fixed(d[ra + mixed_addr(kk, op.nc, op.cdim, op.cst)], shift);
       int dig[OZ_MAXS];
 #pragma unroll
       for (int t = OZ_MAXS - 1; t >= 1; t--) {
@@ -188,7 +195,6 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OzSide S, int32_t s, int3
     }
   }
 }
-
 // ---------------------------------------------------------------- conversion
 // T * 2^e as a correctly rounded double, integer operations only (the rare
 // out-of-range exponents take the FP64 path).
@@ -262,12 +268,19 @@ __device__ __forceinline__ int oz_to_int(float x, float scale) {
   return __float2int_rn(y);
 }
 
+
 struct OzTile {
+  const OzJob *J;
   int64_t o, mt, nt, m, n, i0, j0, seg0, seg1, ksum;
   int32_t ga, gb, nmma;
 };
 
-__device__ __forceinline__ void oz_decode(const OzJob &J, int64_t t, OzTile &T) {
+// Global tile t of the launch -> its job and (output block, row tile, column tile).
+__device__ __forceinline__ void oz_decode(const OzLaunch &L, int64_t t, OzTile &T) {
+  const int64_t j = oz_find(L.job_tile_start, L.n_jobs, t);
+  const OzJob &J = L.jobs[j];
+  T.J = &J;
+  t -= L.job_tile_start[j];
   T.o = oz_find(J.tile_start, J.g.n_out, t);
   T.seg0 = J.g.seg[T.o];
   T.seg1 = J.g.seg[T.o + 1];
@@ -288,16 +301,17 @@ __device__ __forceinline__ void oz_decode(const OzJob &J, int64_t t, OzTile &T) 
   T.ksum = J.ksum[T.o];
 }
 
-__global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
+__global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full_bar[OZ_MAX_STAGES], empty_bar[OZ_MAX_STAGES];
   __shared__ __align__(8) uint64_t acc_full, acc_empty, done_bar;
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_flag;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int s = J.s, NS = J.nstages;
-  const uint32_t a_bytes_max = (uint32_t)s * (OZ_M / 8) * 256;
-  const uint32_t stage_bytes = (uint32_t)s * ((OZ_M + OZ_N) / 8) * 256;
+  const int NS = L.nstages;
+  // stages are sized for the largest slice count of the batch
+  const uint32_t a_bytes_max = (uint32_t)L.s_max * (OZ_M / 8) * 256;
+  const uint32_t stage_bytes = (uint32_t)L.s_max * ((OZ_M + OZ_N) / 8) * 256;
 
   if (threadIdx.x == 0) {
     for (int q = 0; q < NS; q++) {
@@ -320,9 +334,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
     // ---------------- producer: one bulk copy per operand per k-step
     if (lane == 0) {
       uint32_t it = 0;
-      for (int64_t t = blockIdx.x; t < J.n_tiles && !abort_flag; t += gridDim.x) {
+      for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
         OzTile T;
-        oz_decode(J, t, T);
+        oz_decode(L, t, T);
+        const OzJob &J = *T.J;
+        const int s = J.s;
         const uint32_t ba = (uint32_t)s * T.ga * 256, bb = (uint32_t)s * T.gb * 256;
         for (int64_t sidx = T.seg0; sidx < T.seg1 && !abort_flag; sidx++) {
           const int64_t p = J.g.perm ? J.g.perm[sidx] : sidx;
@@ -333,7 +349,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
           for (int64_t q = 0; q < nk; q++, it++) {
             const uint32_t st = it % NS, use = it / NS;
             if (use > 0 && !mbar_wait(&empty_bar[st], (use - 1) & 1)) {
-              atomicOr(J.err, 1);
+              atomicOr(L.err, 1);
               abort_flag = 1;
               break;
             }
@@ -347,16 +363,17 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
       // drain: every copy issued must land before the CTA may exit
       const uint32_t first = it > (uint32_t)NS ? it - NS : 0;
       for (uint32_t q = first; q < it; q++) {
-        if (!mbar_wait(&full_bar[q % NS], (q / NS) & 1)) atomicOr(J.err, 2);
+        if (!mbar_wait(&full_bar[q % NS], (q / NS) & 1)) atomicOr(L.err, 2);
       }
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer
     if (lane == 0) {
       uint32_t it = 0, f = 0;
-      for (int64_t t = blockIdx.x; t < J.n_tiles && !abort_flag; t += gridDim.x) {
+      for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
         OzTile T;
-        oz_decode(J, t, T);
+        oz_decode(L, t, T);
+        const OzJob &J = *T.J;
         const uint32_t idesc = idesc_bf16_f32(OZ_M, (uint32_t)T.nmma);
         int kc = 0;
         for (int64_t sidx = T.seg0; sidx < T.seg1 && !abort_flag; sidx++) {
@@ -365,21 +382,21 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
           for (int64_t q = 0; q < nk; q++, it++) {
             const uint32_t st = it % NS, use = it / NS;
             if (!mbar_wait(&full_bar[st], use & 1)) {
-              atomicOr(J.err, 4);
+              atomicOr(L.err, 4);
               abort_flag = 1;
               break;
             }
             tc_fence_after();
             if (kc == 0) {
               if (f > 0 && !mbar_wait(&acc_empty, (f - 1) & 1)) {
-                atomicOr(J.err, 8);
+                atomicOr(L.err, 8);
                 abort_flag = 1;
                 break;
               }
               tc_fence_after();
             }
             const uint32_t sa = smem_u32(smem + st * stage_bytes);
-            oz_issue_s(s, tmem, smem_desc(sa, 128, 256), smem_desc(sa + a_bytes_max, 128, 256),
+            oz_issue_s(J.s, tmem, smem_desc(sa, 128, 256), smem_desc(sa + a_bytes_max, 128, 256),
                        (uint32_t)T.ga * 16, (uint32_t)T.gb * 16, idesc, kc == 0);
             mma_commit(&empty_bar[st]);
             if (++kc == OZ_CHUNK) {
@@ -396,7 +413,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
       }
       // every MMA issued must finish before TMEM is released
       mma_commit(&done_bar);
-      if (!mbar_wait(&done_bar, 0)) atomicOr(J.err, 32);
+      if (!mbar_wait(&done_bar, 0)) atomicOr(L.err, 32);
     }
   } else {
     // ---------------- epilogue: 8 warps; warp -> TMEM lane quarter, column half
@@ -405,11 +422,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
     const int row = 32 * q4 + lane;
     const uint32_t lane_addr = tmem + ((uint32_t)(32 * q4) << 16);
     const int cbase = half * (OZ_N / 2);
-    const int n_acc = s < OZ_NACC ? s : OZ_NACC;  // accumulators the slice products reach
     uint32_t f = 0;
-    for (int64_t t = blockIdx.x; t < J.n_tiles && !abort_flag; t += gridDim.x) {
+    for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
       OzTile T;
-      oz_decode(J, t, T);
+      oz_decode(L, t, T);
+      const OzJob &J = *T.J;
+      const int n_acc = J.s < OZ_NACC ? J.s : OZ_NACC;  // accumulators the products reach
       const int64_t nflush = (T.ksum + OZ_CHUNK - 1) / OZ_CHUNK;
       const int64_t grow = T.mt * OZ_M + row;
       const bool row_ok = grow < T.m;
@@ -436,7 +454,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
       for (int y = 0; y < OZ_N / 2; y++) S[y] = 0;
       for (int64_t c = 0; c < nflush; c++, f++) {
         if (!mbar_wait(&acc_full, f & 1)) {
-          atomicOr(J.err, 16);
+          atomicOr(L.err, 16);
           abort_flag = 1;
           break;
         }
@@ -464,13 +482,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzJob J) {
       if (abort_flag) break;
       // C = S * 2^(e_r + f_c - 16 - u)
       double *C = (double *)J.g.C + J.g.c_off[T.o];
-      const int64_t *rowB = J.rowB + J.keyB[T.j0];
+      const int64_t rowB = J.rowB[J.keyB[T.j0]];
       if (row_ok) {
 #pragma unroll
         for (int y = 0; y < OZ_N / 2; y++) {
           const int64_t gcol = T.nt * OZ_N + cbase + y;
           if (gcol < T.n) {
-            const int fc = J.expB[*rowB + gcol];
+            const int fc = J.expB[rowB + gcol];
             C[grow + gcol * T.m] = oz_i64_ldexp(S[y], er + fc - 16 - u);
           }
         }
@@ -492,37 +510,101 @@ int oz_stages(int s) {
   return n > OZ_MAX_STAGES ? OZ_MAX_STAGES : n;
 }
 
-tq_status launch_ozaki_prepare(const OzJob &job, const OzSide &SA, const OzSide &SB,
-                               int64_t rowsA, int64_t rowsB, int64_t tilesA, int64_t tilesB,
-                               int32_t *expA, int32_t *expB, int64_t nexpA, int64_t nexpB,
-                               cudaStream_t st) {
+static tq_status oz_setup(int *sms);
+
+tq_status oz_batch_build(const std::vector<OzJob> &jobs, const std::vector<OzSide> &sides,
+                         cudaStream_t st, OzBatchDev &out) {
+  TQ_CHECK(oz_setup(&out.sms));
+  const int64_t nj = (int64_t)jobs.size(), ns = (int64_t)sides.size();
+  std::vector<int64_t> pre((nj + 1) + 3 * (ns + 1), 0);
+  int64_t *jt = pre.data(), *sr = jt + nj + 1, *stl = sr + ns + 1, *se = stl + ns + 1;
+  int s_max = 1;
+  for (int64_t j = 0; j < nj; j++) {
+    jt[j + 1] = jt[j] + jobs[j].n_tiles;
+    s_max = jobs[j].s > s_max ? jobs[j].s : s_max;
+  }
+  for (int64_t k = 0; k < ns; k++) {
+    sr[k + 1] = sr[k] + sides[k].n_rows;
+    stl[k + 1] = stl[k] + sides[k].n_tiles;
+    se[k + 1] = se[k] + sides[k].n_exps;
+  }
+  TQ_CHECK(out.jobs.alloc(std::max<int64_t>(nj, 1), st));
+  TQ_CHECK(out.sides.alloc(std::max<int64_t>(ns, 1), st));
+  TQ_CHECK(out.prefixes.alloc(pre.size(), st));
+  TQ_CHECK(out.err.alloc(1, st));
+  if (nj) TQ_CUDA(cudaMemcpyAsync(out.jobs.p, jobs.data(), nj * sizeof(OzJob),
+                                  cudaMemcpyHostToDevice, st));
+  if (ns) TQ_CUDA(cudaMemcpyAsync(out.sides.p, sides.data(), ns * sizeof(OzSide),
+                                  cudaMemcpyHostToDevice, st));
+  TQ_CUDA(cudaMemcpyAsync(out.prefixes.p, pre.data(), pre.size() * 8, cudaMemcpyHostToDevice, st));
+  TQ_CUDA(cudaMemsetAsync(out.err.p, 0, 4, st));
+  TQ_CUDA(cudaStreamSynchronize(st));  // the host vectors die here
+  OzLaunch &L = out.L;
+  L.jobs = out.jobs.p;
+  L.job_tile_start = out.prefixes.p;
+  L.n_jobs = (int32_t)nj;
+  L.n_tiles = jt[nj];
+  L.sides = out.sides.p;
+  L.side_row_start = out.prefixes.p + (nj + 1);
+  L.side_tile_start = L.side_row_start + (ns + 1);
+  L.side_exp_start = L.side_tile_start + (ns + 1);
+  L.n_sides = (int32_t)ns;
+  L.n_rows = sr[ns];
+  L.n_slice_tiles = stl[ns];
+  L.n_exps = se[ns];
+  L.s_max = s_max;
+  L.nstages = oz_stages(s_max);
+  L.err = out.err.p;
+  return TQ_OK;
+}
+
+tq_status oz_batch_prepare(const OzBatchDev &b, cudaStream_t st) {
+  const OzLaunch &L = b.L;
   const int T = 256;
-  if (nexpA) count_launch(), oz_exp_init_kernel<<<(unsigned)((nexpA + T - 1) / T), T, 0, st>>>(expA, nexpA);
-  if (nexpB) count_launch(), oz_exp_init_kernel<<<(unsigned)((nexpB + T - 1) / T), T, 0, st>>>(expB, nexpB);
-  if (rowsA) count_launch(), oz_rowexp_kernel<<<(unsigned)((rowsA + T - 1) / T), T, 0, st>>>(SA, rowsA, expA);
-  if (rowsB) count_launch(), oz_rowexp_kernel<<<(unsigned)((rowsB + T - 1) / T), T, 0, st>>>(SB, rowsB, expB);
-  TQ_CUDA(cudaGetLastError());
-  if (tilesA) count_launch(), oz_slice_kernel<<<(unsigned)tilesA, 256, 0, st>>>(SA, job.s, OZ_M, expA,
-                                                                  (uint8_t *)job.sliceA);
-  if (tilesB) count_launch(), oz_slice_kernel<<<(unsigned)tilesB, 256, 0, st>>>(SB, job.s, OZ_N, expB,
-                                                                  (uint8_t *)job.sliceB);
+  if (L.n_exps) count_launch(), oz_exp_init_kernel<<<(unsigned)((L.n_exps + T - 1) / T), T, 0, st>>>(L);
+  if (L.n_rows) count_launch(), oz_rowexp_kernel<<<(unsigned)((L.n_rows + T - 1) / T), T, 0, st>>>(L);
+  if (L.n_slice_tiles) count_launch(), oz_slice_kernel<<<(unsigned)L.n_slice_tiles, 256, 0, st>>>(L);
   TQ_CUDA(cudaGetLastError());
   return TQ_OK;
 }
 
-tq_status launch_ozaki_gemm(const OzJob &job, cudaStream_t st) {
-  if (job.n_tiles == 0) return TQ_OK;
-  static int sms = 0;
-  if (!sms) {
-    int dev;
-    TQ_CUDA(cudaGetDevice(&dev));
-    TQ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+// Device attributes and the kernel's shared-memory opt-in, once per device and
+// before any stream capture (called when a batch is built).
+static int g_sms[128] = {0};
+
+static tq_status oz_setup(int *sms) {
+  int dev = 0;
+  TQ_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return fail(TQ_ERR_UNSUPPORTED, "device ordinal above 127");
+  if (!g_sms[dev]) {
+    int n = 0;
+    TQ_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
     TQ_CUDA(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  OZ_SMEM_BYTES));
+    g_sms[dev] = n;
   }
-  const int64_t grid = job.n_tiles < sms ? job.n_tiles : sms;
-  count_launch(), oz_gemm_kernel<<<(unsigned)grid, OZ_THREADS, OZ_SMEM_BYTES, st>>>(job);
+  *sms = g_sms[dev];
+  return TQ_OK;
+}
+
+tq_status oz_batch_gemm(const OzBatchDev &b, cudaStream_t st) {
+  const OzLaunch &L = b.L;
+  if (L.n_tiles == 0) return TQ_OK;
+  const int64_t grid = L.n_tiles < b.sms ? L.n_tiles : b.sms;
+  count_launch(), oz_gemm_kernel<<<(unsigned)grid, OZ_THREADS, OZ_SMEM_BYTES, st>>>(L);
   TQ_CUDA(cudaGetLastError());
+  return TQ_OK;
+}
+
+tq_status oz_batch_check(const OzBatchDev &b, cudaStream_t st) {
+  int32_t e = 0;
+  TQ_CUDA(cudaMemcpyAsync(&e, b.err.p, 4, cudaMemcpyDeviceToHost, st));
+  TQ_CUDA(cudaStreamSynchronize(st));
+  if (e) {
+    TQ_CUDA(cudaMemsetAsync(b.err.p, 0, 4, st));
+    return fail(TQ_ERR_TIMEOUT,
+                "a tensor-core pipeline wait gave up (flags " + std::to_string(e) + ")");
+  }
   return TQ_OK;
 }
 

@@ -1,4 +1,6 @@
-// Work description of the tensor-core (sliced) forms of the grouped GEMM.
+// Work description of the tensor-core (sliced) forms of the grouped GEMM.  A
+// launch covers a batch of contractions ("jobs"): one contraction is a batch of
+// one; many independent contractions share one persistent launch.
 #pragma once
 #include "gemm.cuh"
 
@@ -11,9 +13,10 @@ constexpr int OZ_MAXS = 7;       // most slices supported
 constexpr int OZ_MAX_STAGES = 8;
 constexpr int OZ_EXP_ZERO = -(1 << 20);  // exponent of an all-zero row
 
-// One operand side (A or B) of the slicing passes: every block of the tensor
-// is one operand unit viewed as a rows x k matrix (rows over the free legs,
-// columns over the contracted legs in pair order, each block's full range).
+// One operand side (A or B) of one job, for the slicing passes: every block of
+// the tensor is one operand unit viewed as a rows x k matrix (rows over the
+// free legs, columns over the contracted legs in pair order, each block's full
+// range).
 struct OzSide {
   DevBS T;
   int32_t nfree, ncon;
@@ -23,6 +26,10 @@ struct OzSide {
   const int64_t *row_start;   // per block: exclusive scan of rows
   const int64_t *tile_start;  // per block: exclusive scan of row tiles
   const int64_t *unit_off;    // per block: slice storage offset, 256-byte units
+  int32_t *exps;              // exponent table
+  uint8_t *slices;            // slice storage
+  int64_t n_rows, n_tiles, n_exps;
+  int32_t s, rt_rows;
 };
 
 struct OzJob {
@@ -36,17 +43,43 @@ struct OzJob {
   const int64_t *keyA, *keyB;
   const int64_t *rowA, *rowB;
   const int32_t *expA, *expB;
-  int32_t s, nstages;
+  int32_t s;
+};
+
+// Kernel parameter of a batched launch (arrays in device memory).
+struct OzLaunch {
+  const OzJob *jobs;
+  const int64_t *job_tile_start;   // [n_jobs+1]
+  int32_t n_jobs;
+  int64_t n_tiles;
+  const OzSide *sides;
+  const int64_t *side_row_start;   // [n_sides+1]
+  const int64_t *side_tile_start;  // [n_sides+1]
+  const int64_t *side_exp_start;   // [n_sides+1]
+  int32_t n_sides;
+  int64_t n_rows, n_slice_tiles, n_exps;
+  int32_t s_max, nstages;
   int32_t *err;
 };
 
+// Device copies of the job and side lists plus their prefix sums.
+struct OzBatchDev {
+  DevArray<OzJob> jobs;
+  DevArray<OzSide> sides;
+  DevArray<int64_t> prefixes;  // job tiles | side rows | side tiles | side exps
+  DevArray<int32_t> err;
+  OzLaunch L{};
+  int sms = 0;  // multiprocessors of the device: the persistent grid
+};
+
 int oz_stages(int s);
-// Row exponents and slices of both operands.
-tq_status launch_ozaki_prepare(const OzJob &job, const OzSide &SA, const OzSide &SB,
-                               int64_t rowsA, int64_t rowsB, int64_t tilesA, int64_t tilesB,
-                               int32_t *expA, int32_t *expB, int64_t nexpA, int64_t nexpB,
-                               cudaStream_t st);
-// The persistent tensor-core GEMM over all output tiles.
-tq_status launch_ozaki_gemm(const OzJob &job, cudaStream_t st);
+tq_status oz_batch_build(const std::vector<OzJob> &jobs, const std::vector<OzSide> &sides,
+                         cudaStream_t s, OzBatchDev &out);
+// Row exponents and slices of every side of the batch.
+tq_status oz_batch_prepare(const OzBatchDev &b, cudaStream_t s);
+// The persistent tensor-core GEMM over every output tile of every job.
+tq_status oz_batch_gemm(const OzBatchDev &b, cudaStream_t s);
+// Reads (and clears) the bounded-wait error flag; synchronises the stream.
+tq_status oz_batch_check(const OzBatchDev &b, cudaStream_t s);
 
 }  // namespace tq

@@ -3,6 +3,7 @@
 #pragma once
 #include <memory>
 
+#include "ozaki.cuh"
 #include "tq_internal.h"
 
 struct tq_plan {
@@ -27,9 +28,12 @@ struct tq_plan {
   tq::DevArray<int64_t> tilestartA, tilestartB;
   tq::DevArray<int64_t> unitA, unitB;          // per block: slice offset / 256 B
   tq::DevArray<int64_t> ksum, tc_tile_start;
-  tq::DevArray<int32_t> expA, expB, nk_pair, err;
+  tq::DevArray<int32_t> expA, expB, nk_pair;
   tq::DevArray<uint8_t> sliceA, sliceB;
   int64_t rowsA = 0, rowsB = 0, tilesA = 0, tilesB = 0, nexpA = 0, nexpB = 0, tc_tiles = 0;
+  tq::OzJob tc_job{};              // this contraction as one job
+  tq::OzSide tc_side[2]{};         // its A and B operand sides
+  tq::OzBatchDev tcb;              // the same as a batch of one, on the device
   // optional phase timing (events on the launching stream)
   bool profile = false;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};

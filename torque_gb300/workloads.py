@@ -86,3 +86,67 @@ def uneven_u1(peak: float = 48.0, qmax: int = 16, seed: int = 2, data: bool = Tr
     B = charge_blocks([leg(+1), leg(+1), leg(-1), leg(-1)])
     return Contraction("u1-rank4-gauss%d-q%d" % (int(peak), 2 * qmax + 1), A, B,
                        np.zeros(0), np.zeros(0), np.array([[2, 0], [3, 1]], np.int64))
+
+
+# ---------------------------------------------------------------- PEPS sweep
+def scaled_sectors(dim: int):
+    """U(1) sectors of a leg of dimension `dim`, Gaussian-profiled like the
+    uneven case and scaled to the dimension: charges -Q..Q with Q = max(1,
+    dim // 12), weights exp(-q^2 / (2 sigma^2)) with sigma = max(1, Q / 2),
+    sizes by largest remainder so they sum to dim, each at least 1."""
+    Q = max(1, dim // 12)
+    q = np.arange(-Q, Q + 1)
+    w = np.exp(-q.astype(float) ** 2 / (2.0 * max(1.0, Q / 2.0) ** 2))
+    raw = w / w.sum() * dim
+    s = np.maximum(1, np.floor(raw)).astype(int)
+    while s.sum() < dim:
+        s[np.argmax(raw - s)] += 1
+    while s.sum() > dim:
+        k = np.argmax(np.where(s > 1, s - raw, -np.inf))
+        s[k] -= 1
+    return q.tolist(), s.tolist()
+
+
+@dataclass
+class SiteUpdate:
+    """One PEPS-sweep site update: E1[chi,l,u,chi'] x T[l,u,r,d,p] over (l,u)
+    gives X[chi,chi',r,d,p]; X x E2[chi',r,d,chi''] over (chi',r,d) gives
+    Y[chi,p,chi'']."""
+    D: int
+    chi: int
+    T: BlockList
+    E1: BlockList
+    E2: BlockList
+    t_data: np.ndarray
+    e1_data: np.ndarray
+    e2_data: np.ndarray
+    pairs1 = np.array([[1, 0], [2, 1]], np.int64)
+    pairs2 = np.array([[1, 0], [2, 1], [3, 2]], np.int64)
+
+
+def peps_sweep(n: int = 256, seed: int = 3, data: bool = True):
+    """n independent site updates: D ~ U{4..10}, chi ~ U{16..64} (drawn first,
+    all instances), then the entries N(0,1), instance by instance, T, E1, E2,
+    from numpy's PCG64 with `seed`.  Directions: T (l,u in; r,d,p out), E1 (chi
+    in, l,u out, chi' in), E2 (chi' out, r,d in, chi'' out); physical leg p has
+    charges {0, 1} of size 1 each."""
+    rng = np.random.default_rng(seed)
+    Ds = rng.integers(4, 11, size=n)
+    chis = rng.integers(16, 65, size=n)
+    out = []
+    for D, chi in zip(Ds.tolist(), chis.tolist()):
+        qd, sd = scaled_sectors(D)
+        qc, sc = scaled_sectors(chi)
+        p = ([0, 1], [1, 1])
+        T = charge_blocks([Leg(qd, sd, +1), Leg(qd, sd, +1), Leg(qd, sd, -1), Leg(qd, sd, -1),
+                           Leg(*p, -1)])
+        E1 = charge_blocks([Leg(qc, sc, +1), Leg(qd, sd, -1), Leg(qd, sd, -1), Leg(qc, sc, +1)])
+        E2 = charge_blocks([Leg(qc, sc, -1), Leg(qd, sd, +1), Leg(qd, sd, +1), Leg(qc, sc, -1)])
+        if data:
+            t = rng.standard_normal(T.n_elem)
+            e1 = rng.standard_normal(E1.n_elem)
+            e2 = rng.standard_normal(E2.n_elem)
+        else:
+            t = e1 = e2 = np.zeros(0)
+        out.append(SiteUpdate(D, chi, T, E1, E2, t, e1, e2))
+    return out
