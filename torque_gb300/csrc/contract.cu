@@ -498,6 +498,7 @@ tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64
 
   tq_bs *C = new_tensor(A->dtype, rc, new_dim.data());
   std::unique_ptr<tq_bs, tq_status (*)(tq_bs *)> Cguard(C, tq_bs_destroy);
+  P->C = C;  // borrowed until the plan is handed out; Cguard owns it on failure
 
   if (rc == 0) {
     // rank-0 result: one scalar, sum over all pairs
