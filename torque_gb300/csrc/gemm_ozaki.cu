@@ -337,15 +337,19 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
         OzTile T;
         oz_decode(L, t, T);
+        // job fields in registers: the asm memory clobbers below would reload them
         const OzJob &J = *T.J;
         const int s = J.s;
+        const int64_t *perm = J.g.perm, *unitA = J.unitA, *unitB = J.unitB;
+        const int32_t *pa = J.g.pa, *pb = J.g.pb, *nk_pair = J.nk_pair;
+        const uint8_t *sliceA = J.sliceA, *sliceB = J.sliceB;
         const uint32_t ba = (uint32_t)s * T.ga * 256, bb = (uint32_t)s * T.gb * 256;
         for (int64_t sidx = T.seg0; sidx < T.seg1 && !abort_flag; sidx++) {
-          const int64_t p = J.g.perm ? J.g.perm[sidx] : sidx;
-          const int64_t i = J.g.pa[p], j = J.g.pb[p];
-          const int64_t nk = J.nk_pair[p];
-          const uint8_t *ga = J.sliceA + 256 * J.unitA[i] + nk * s * 256 * (OZ_M / 8) * T.mt;
-          const uint8_t *gb = J.sliceB + 256 * J.unitB[j] + nk * s * 256 * (OZ_N / 8) * T.nt;
+          const int64_t p = perm ? perm[sidx] : sidx;
+          const int64_t i = pa[p], j = pb[p];
+          const int64_t nk = nk_pair[p];
+          const uint8_t *ga = sliceA + 256 * unitA[i] + nk * s * 256 * (OZ_M / 8) * T.mt;
+          const uint8_t *gb = sliceB + 256 * unitB[j] + nk * s * 256 * (OZ_N / 8) * T.nt;
           for (int64_t q = 0; q < nk; q++, it++) {
             const uint32_t st = it % NS, use = it / NS;
             if (use > 0 && !mbar_wait(&empty_bar[st], (use - 1) & 1)) {
@@ -374,11 +378,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         OzTile T;
         oz_decode(L, t, T);
         const OzJob &J = *T.J;
+        const int s = J.s;
+        const int64_t *perm = J.g.perm;
+        const int32_t *nk_pair = J.nk_pair;
         const uint32_t idesc = idesc_bf16_f32(OZ_M, (uint32_t)T.nmma);
         int kc = 0;
         for (int64_t sidx = T.seg0; sidx < T.seg1 && !abort_flag; sidx++) {
-          const int64_t p = J.g.perm ? J.g.perm[sidx] : sidx;
-          const int64_t nk = J.nk_pair[p];
+          const int64_t p = perm ? perm[sidx] : sidx;
+          const int64_t nk = nk_pair[p];
           for (int64_t q = 0; q < nk; q++, it++) {
             const uint32_t st = it % NS, use = it / NS;
             if (!mbar_wait(&full_bar[st], use & 1)) {
@@ -396,7 +403,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
               tc_fence_after();
             }
             const uint32_t sa = smem_u32(smem + st * stage_bytes);
-            oz_issue_s(J.s, tmem, smem_desc(sa, 128, 256), smem_desc(sa + a_bytes_max, 128, 256),
+            oz_issue_s(s, tmem, smem_desc(sa, 128, 256), smem_desc(sa + a_bytes_max, 128, 256),
                        (uint32_t)T.ga * 16, (uint32_t)T.gb * 16, idesc, kc == 0);
             mma_commit(&empty_bar[st]);
             if (++kc == OZ_CHUNK) {
@@ -483,12 +490,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       // C = S * 2^(e_r + f_c - 16 - u)
       double *C = (double *)J.g.C + J.g.c_off[T.o];
       const int64_t rowB = J.rowB[J.keyB[T.j0]];
+      const int32_t *expB = J.expB;
       if (row_ok) {
 #pragma unroll
         for (int y = 0; y < OZ_N / 2; y++) {
           const int64_t gcol = T.nt * OZ_N + cbase + y;
           if (gcol < T.n) {
-            const int fc = J.expB[rowB + gcol];
+            const int fc = expB[rowB + gcol];
             C[grow + gcol * T.m] = oz_i64_ldexp(S[y], er + fc - 16 - u);
           }
         }
