@@ -11,17 +11,18 @@
 //     digits d_0..d_{s-1} in [-128, 128]; slice t is stored as the bf16 value
 //     d_t * 2^(-8t) (exact: at most 8 significant bits);
 //   * the slice products A_t B_u^T with t+u <= s-1 run on the tensor cores with
-//     fp32 accumulation in TMEM, in five accumulators by g = t+u: D0..D3
-//     (g = 0..3) hold multiples of 2^(-8g) below (g+1) K 2^14 2^(-8g), whole
-//     numbers of 24 bits or fewer for K <= 240, so the tensor core sums them
-//     exactly; D4 (g >= 4, at most 2^-32 of D0) is rounded.  Every 240 columns
-//     of the fused K (all pairs of the output block, in order) the five are
-//     folded into an int64 running sum S = sum_a round(2^24 D_a) held in the
-//     epilogue's registers (exact but for D4's rounding; below 2^60 for a fused
-//     K up to 2^20).  A single fp32 accumulator for the lower groups is not
-//     enough: the tensor core's fp32 accumulation truncates, which loses about
-//     K ulps of the group it holds.
-//   * C = S * 2^(e_r + f_c - 40), converted to FP64 with integer operations.
+//     fp32 accumulation in TMEM, in four accumulators by g = t+u: D0..D2
+//     (g = 0..2) hold multiples of 2^(-8g) below (g+1) K 2^14 2^(-8g), whole
+//     numbers of 24 bits or fewer for K <= 336, so the tensor core sums them
+//     exactly; D3 (g >= 3, at most 2^-24 of D0) is rounded.  Each accumulator is
+//     retired after at most 336 columns of the fused K (all pairs of the output
+//     block, in order) on a staggered schedule and restarted in a spare TMEM
+//     slot, while the epilogue folds the retired slot into an int64 running sum
+//     S = sum round(2^u D_a) held in registers (u per tile, so no data can
+//     overflow it) — the MMAs do not wait for the fold.  A single fp32
+//     accumulator for the lower groups is not enough: the tensor core's fp32
+//     accumulation truncates, which loses about K ulps of the group it holds.
+//   * C = S * 2^(e_r + f_c - 16 - u), converted to FP64 with integer operations.
 // No FP64 arithmetic runs in the GEMM: GB300 issues about 2 FP64 FMAs per SM
 // per clock against ~4000 bf16 FMAs, so FP64 work stays in the row-exponent
 // pass (one ilogb per row) only.
@@ -43,9 +44,8 @@ namespace tq {
 
 constexpr int OZ_THREADS = 320;  // warp 0: loads, warp 1: MMA, warps 2-9: epilogue
 constexpr uint32_t OZ_TMEM_COLS = 512;
-// TMEM columns: accumulator D_a (a = 0..4) at [a*OZ_N, (a+1)*OZ_N), 480 of 512
-constexpr int OZ_NACC = 5;
-static_assert(OZ_NACC * OZ_N <= (int)OZ_TMEM_COLS, "accumulators exceed TMEM");
+// TMEM: OZ_NACC + 1 slots of OZ_N columns (480 of 512)
+constexpr int OZ_NACC = 4;
 constexpr int OZ_SMEM_BYTES = 200 * 1024;
 
 __device__ __forceinline__ int64_t oz_find(const int64_t *start, int64_t n, int64_t t) {
@@ -224,14 +224,28 @@ __device__ __forceinline__ double oz_i64_ldexp(long long T, int e) {
 }
 
 // ---------------------------------------------------------------- the GEMM
+// Accumulators by g = t+u: D0, D1, D2 (exact) and D3 (g >= 3, rounded).  They
+// live in OZ_NSLOT TMEM slots of OZ_N columns, one more slot than accumulators:
+// accumulator a is retired after every OZ_CHUNK k-steps on its own staggered
+// schedule (first after OZ_CHUNK - OZ_STAG*a), moved into the spare slot, and
+// the retired slot is drained by the epilogue while the MMAs go on.  Each slot
+// has its own full/empty barrier pair, so no parity wait can fall two phases
+// behind: a slot is never retired twice without a drain in between.
+constexpr int OZ_NSLOT = OZ_NACC + 1;
+constexpr int OZ_STAG = 5;
+constexpr int OZ_FINAL = 100;
+static_assert(OZ_NSLOT * OZ_N <= (int)OZ_TMEM_COLS, "slots exceed TMEM");
+static_assert(OZ_STAG * (OZ_NACC - 1) < OZ_CHUNK, "stagger must fit one chunk");
+
 // All slice products of one k-step, fully unrolled: product (t, u) goes to
-// accumulator min(t+u, OZ_NACC-1).  Descriptors advance by whole row groups
-// (the start-address field counts 16-byte units).  On the first k-step of a
-// flush chunk the first product into each accumulator overwrites it.
+// accumulator min(t+u, OZ_NACC-1) at TMEM column slot[acc].  Descriptors advance
+// by whole row groups (the start-address field counts 16-byte units).  The first
+// product of the k-step into an accumulator whose bit is set in `fresh`
+// overwrites it.
 template <int S>
-__device__ __forceinline__ void oz_issue(uint32_t tmem, uint64_t da0, uint64_t db0,
-                                         uint32_t a_step, uint32_t b_step, uint32_t idesc,
-                                         bool chunk_start) {
+__device__ __forceinline__ void oz_issue(const uint32_t (&col)[OZ_NACC], uint64_t da0,
+                                         uint64_t db0, uint32_t a_step, uint32_t b_step,
+                                         uint32_t idesc, uint32_t fresh) {
 #pragma unroll
   for (int t = 0; t < S; t++) {
 #pragma unroll
@@ -239,25 +253,54 @@ __device__ __forceinline__ void oz_issue(uint32_t tmem, uint64_t da0, uint64_t d
       const int acc = t + u < OZ_NACC - 1 ? t + u : OZ_NACC - 1;
       // first (t, u) in this order that lands in accumulator acc
       const bool first = acc < OZ_NACC - 1 ? t == 0 : (t == 0 && u == OZ_NACC - 1);
-      mma_bf16(tmem + acc * OZ_N, da0 + (uint64_t)(t * a_step), db0 + (uint64_t)(u * b_step),
-               idesc, (chunk_start && first) ? 0u : 1u);
+      const uint32_t keep = (first && ((fresh >> acc) & 1)) ? 0u : 1u;
+      mma_bf16(col[acc], da0 + (uint64_t)(t * a_step), db0 + (uint64_t)(u * b_step), idesc, keep);
     }
   }
 }
 
-__device__ __forceinline__ void oz_issue_s(int s, uint32_t tmem, uint64_t da0, uint64_t db0,
-                                           uint32_t a_step, uint32_t b_step, uint32_t idesc,
-                                           bool chunk_start) {
+__device__ __forceinline__ void oz_issue_s(int s, const uint32_t (&col)[OZ_NACC], uint64_t da0,
+                                           uint64_t db0, uint32_t a_step, uint32_t b_step,
+                                           uint32_t idesc, uint32_t fresh) {
   switch (s) {
-    case 1: oz_issue<1>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
-    case 2: oz_issue<2>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
-    case 3: oz_issue<3>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
-    case 4: oz_issue<4>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
-    case 5: oz_issue<5>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
-    case 6: oz_issue<6>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
-    default: oz_issue<7>(tmem, da0, db0, a_step, b_step, idesc, chunk_start); break;
+    case 1: oz_issue<1>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    case 2: oz_issue<2>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    case 3: oz_issue<3>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    case 4: oz_issue<4>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    case 5: oz_issue<5>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    case 6: oz_issue<6>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    default: oz_issue<7>(col, da0, db0, a_step, b_step, idesc, fresh); break;
   }
 }
+
+// Retirement schedule of a tile with ksum k-steps: next event after k-step k.
+// Returns the k-step (1-based) of the next event and its kind (accumulator
+// index, or OZ_FINAL at the end of the tile, which retires every accumulator).
+struct OzSchedule {
+  int64_t next[OZ_NACC];
+  int64_t ksum;
+  int n_acc;
+  __device__ __forceinline__ void start(int64_t ks, int na) {
+    ksum = ks;
+    n_acc = na;
+#pragma unroll
+    for (int a = 0; a < OZ_NACC; a++) next[a] = OZ_CHUNK - OZ_STAG * a;
+  }
+  // event at or after the current position: (k, kind)
+  __device__ __forceinline__ void peek(int64_t &k, int &kind) const {
+    k = ksum;
+    kind = OZ_FINAL;
+#pragma unroll
+    for (int a = 0; a < OZ_NACC; a++)
+      if (a < n_acc && next[a] < k) {
+        k = next[a];
+        kind = a;
+      }
+  }
+  __device__ __forceinline__ void advance(int kind) {
+    if (kind != OZ_FINAL) next[kind] += OZ_CHUNK;
+  }
+};
 
 // Exact fp32 -> int32 for values whose scaled magnitude is below 2^22 (one FMA
 // against 1.5 * 2^23, whose ulp is 1, then an integer subtract; rounds to
@@ -267,7 +310,6 @@ __device__ __forceinline__ int oz_to_int(float x, float scale) {
   if (fabsf(y) < 4194304.0f) return __float_as_int(y + 12582912.0f) - 0x4B400000;
   return __float2int_rn(y);
 }
-
 
 struct OzTile {
   const OzJob *J;
@@ -304,7 +346,7 @@ __device__ __forceinline__ void oz_decode(const OzLaunch &L, int64_t t, OzTile &
 __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full_bar[OZ_MAX_STAGES], empty_bar[OZ_MAX_STAGES];
-  __shared__ __align__(8) uint64_t acc_full, acc_empty, done_bar;
+  __shared__ __align__(8) uint64_t slot_full[OZ_NSLOT], slot_empty[OZ_NSLOT], done_bar;
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_flag;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -318,8 +360,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       mbar_init(&full_bar[q], 1);
       mbar_init(&empty_bar[q], 1);
     }
-    mbar_init(&acc_full, 1);
-    mbar_init(&acc_empty, 8);
+    for (int q = 0; q < OZ_NSLOT; q++) {
+      mbar_init(&slot_full[q], 1);
+      mbar_init(&slot_empty[q], 8);
+    }
     mbar_init(&done_bar, 1);
     abort_flag = 0;
     fence_mbar_init();
@@ -373,16 +417,29 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
   } else if (warp == 1) {
     // ---------------- MMA issuer
     if (lane == 0) {
-      uint32_t it = 0, f = 0;
+      uint32_t it = 0;
+      // slot of accumulator a in bits [3a, 3a+3); per slot p: bit p of `par` is
+      // the parity of its completed uses, bit p of `used` whether it had one
+      uint32_t map = 0, par = 0, used = 0;
+      int spare = OZ_NACC;
+#pragma unroll
+      for (int a = 0; a < OZ_NACC; a++) map |= (uint32_t)a << (3 * a);
       for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
         OzTile T;
         oz_decode(L, t, T);
         const OzJob &J = *T.J;
         const int s = J.s;
+        const int n_acc = s < OZ_NACC ? s : OZ_NACC;
         const int64_t *perm = J.g.perm;
         const int32_t *nk_pair = J.nk_pair;
         const uint32_t idesc = idesc_bf16_f32(OZ_M, (uint32_t)T.nmma);
-        int kc = 0;
+        OzSchedule sch;
+        sch.start(T.ksum, n_acc);
+        int64_t ev_k;
+        int ev_kind;
+        sch.peek(ev_k, ev_kind);
+        uint32_t fresh = (1u << n_acc) - 1;  // accumulators to (re)start in a free slot
+        int64_t k = 0;
         for (int64_t sidx = T.seg0; sidx < T.seg1 && !abort_flag; sidx++) {
           const int64_t p = perm ? perm[sidx] : sidx;
           const int64_t nk = nk_pair[p];
@@ -393,29 +450,49 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
               abort_flag = 1;
               break;
             }
-            tc_fence_after();
-            if (kc == 0) {
-              if (f > 0 && !mbar_wait(&acc_empty, (f - 1) & 1)) {
-                atomicOr(L.err, 8);
-                abort_flag = 1;
-                break;
-              }
-              tc_fence_after();
+            // a slot taken up again must have been drained since its last use
+            bool ok = true;
+#pragma unroll
+            for (int a = 0; a < OZ_NACC; a++) {
+              const uint32_t p = (map >> (3 * a)) & 7;
+              if (((fresh >> a) & 1) && ((used >> p) & 1) &&
+                  !mbar_wait(&slot_empty[p], ((par >> p) & 1) ^ 1))
+                ok = false;
             }
+            if (!ok) {
+              atomicOr(L.err, 8);
+              abort_flag = 1;
+              break;
+            }
+            tc_fence_after();
+            uint32_t col[OZ_NACC];
+#pragma unroll
+            for (int a = 0; a < OZ_NACC; a++) col[a] = tmem + ((map >> (3 * a)) & 7) * OZ_N;
             const uint32_t sa = smem_u32(smem + st * stage_bytes);
-            oz_issue_s(s, tmem, smem_desc(sa, 128, 256), smem_desc(sa + a_bytes_max, 128, 256),
-                       (uint32_t)T.ga * 16, (uint32_t)T.gb * 16, idesc, kc == 0);
+            oz_issue_s(s, col, smem_desc(sa, 128, 256), smem_desc(sa + a_bytes_max, 128, 256),
+                       (uint32_t)T.ga * 16, (uint32_t)T.gb * 16, idesc, fresh);
             mma_commit(&empty_bar[st]);
-            if (++kc == OZ_CHUNK) {
-              mma_commit(&acc_full);
-              f++;
-              kc = 0;
+            fresh = 0;
+            if (++k == ev_k) {
+#pragma unroll
+              for (int a = 0; a < OZ_NACC; a++) {
+                if (a >= n_acc || (ev_kind != OZ_FINAL && a != ev_kind)) continue;
+                const uint32_t p = (map >> (3 * a)) & 7;
+                mma_commit(&slot_full[p]);
+                par ^= 1u << p;
+                used |= 1u << p;
+                if (ev_kind != OZ_FINAL) {  // restart a in the spare slot
+                  map = (map & ~(7u << (3 * a))) | ((uint32_t)spare << (3 * a));
+                  spare = (int)p;
+                  fresh |= 1u << a;
+                }
+              }
+              if (ev_kind != OZ_FINAL) {
+                sch.advance(ev_kind);
+                sch.peek(ev_k, ev_kind);
+              }
             }
           }
-        }
-        if (kc > 0 && !abort_flag) {
-          mma_commit(&acc_full);
-          f++;
         }
       }
       // every MMA issued must finish before TMEM is released
@@ -429,62 +506,72 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
     const int row = 32 * q4 + lane;
     const uint32_t lane_addr = tmem + ((uint32_t)(32 * q4) << 16);
     const int cbase = half * (OZ_N / 2);
-    uint32_t f = 0;
+    // the MMA warp's slot map, replayed: accumulator a in bits [3a, 3a+3),
+    // bit p of `par` = parity of the drains of slot p so far
+    uint32_t map = 0, par = 0;
+    int spare = OZ_NACC;
+#pragma unroll
+    for (int a = 0; a < OZ_NACC; a++) map |= (uint32_t)a << (3 * a);
     for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
       OzTile T;
       oz_decode(L, t, T);
       const OzJob &J = *T.J;
-      const int n_acc = J.s < OZ_NACC ? J.s : OZ_NACC;  // accumulators the products reach
-      const int64_t nflush = (T.ksum + OZ_CHUNK - 1) / OZ_CHUNK;
+      const int n_acc = J.s < OZ_NACC ? J.s : OZ_NACC;
       const int64_t grow = T.mt * OZ_M + row;
       const bool row_ok = grow < T.m;
       const int er = row_ok ? J.expA[J.rowA[J.keyA[T.i0]] + grow] : 0;
       // S: running sum in units of 2^-u of the leading slice product.  With
       // u <= 48 - log2(K) the sum stays below 2^62.1 for any data, and u >= 24
-      // keeps D0..D3 (whole multiples of 2^-24) exact.
+      // keeps D0..D2 (whole multiples of 2^-16) exact.
       int kb = 0;
       while (kb < 40 && (int64_t(1) << kb) < 16 * T.ksum) kb++;
       const int u = 48 - kb < 32 ? 48 - kb : 32;
-      // D_a (a < 4) holds multiples of 2^-8a below 2^24 * 2^-8a: D_a 2^8a is a
-      // whole number of int32; D4 is rounded at 2^-u
-      float scale[OZ_NACC];
-      int shift[OZ_NACC];
-#pragma unroll
-      for (int a = 0; a < OZ_NACC - 1; a++) {
-        scale[a] = __int_as_float((127 + 8 * a) << 23);
-        shift[a] = u - 8 * a;
-      }
-      scale[OZ_NACC - 1] = __int_as_float((127 + u) << 23);
-      shift[OZ_NACC - 1] = 0;
       long long S[OZ_N / 2];
 #pragma unroll
       for (int y = 0; y < OZ_N / 2; y++) S[y] = 0;
-      for (int64_t c = 0; c < nflush; c++, f++) {
-        if (!mbar_wait(&acc_full, f & 1)) {
-          atomicOr(L.err, 16);
-          abort_flag = 1;
-          break;
-        }
-        tc_fence_after();
-        // one 8-column chunk of every accumulator per round, a single wait
+      OzSchedule sch;
+      sch.start(T.ksum, n_acc);
+      bool done = false;
+      while (!done && !abort_flag) {
+        int64_t ev_k;
+        int ev_kind;
+        sch.peek(ev_k, ev_kind);
+        done = ev_kind == OZ_FINAL;
+        // drain the retired slot(s): D_a (a < 3) holds multiples of 2^-8a below
+        // 2^24 * 2^-8a, so D_a 2^8a is a whole int32; D3 is rounded at 2^-u
 #pragma unroll
-        for (int x = 0; x < OZ_N / 16; x++) {
-          uint32_t v[OZ_NACC][8];
+        for (int a = 0; a < OZ_NACC; a++) {
+          if (a >= n_acc || (!done && a != ev_kind)) continue;
+          const uint32_t p = (map >> (3 * a)) & 7;
+          if (!mbar_wait(&slot_full[p], (par >> p) & 1)) {
+            atomicOr(L.err, 16);
+            abort_flag = 1;
+            break;
+          }
+          tc_fence_after();
+          const float scale = a < OZ_NACC - 1 ? __int_as_float((127 + 8 * a) << 23)
+                                              : __int_as_float((127 + u) << 23);
+          const int shift = a < OZ_NACC - 1 ? u - 8 * a : 0;
+          uint32_t v[OZ_N / 16][8];
 #pragma unroll
-          for (int a = 0; a < OZ_NACC; a++)
-            if (a < n_acc) tmem_ld8(lane_addr + a * OZ_N + cbase + 8 * x, v[a]);
+          for (int x = 0; x < OZ_N / 16; x++)
+            tmem_ld8(lane_addr + p * OZ_N + cbase + 8 * x, v[x]);
           tmem_ld_wait();
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&slot_empty[p]);
+          par ^= 1u << p;
 #pragma unroll
-          for (int a = 0; a < OZ_NACC; a++) {
-            if (a >= n_acc) break;
+          for (int x = 0; x < OZ_N / 16; x++)
 #pragma unroll
             for (int y = 0; y < 8; y++)
-              S[8 * x + y] += (long long)oz_to_int(__uint_as_float(v[a][y]), scale[a]) << shift[a];
+              S[8 * x + y] += (long long)oz_to_int(__uint_as_float(v[x][y]), scale) << shift;
+          if (!done) {
+            map = (map & ~(7u << (3 * a))) | ((uint32_t)spare << (3 * a));
+            spare = (int)p;
+            sch.advance(a);
           }
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&acc_empty);
       }
       if (abort_flag) break;
       // C = S * 2^(e_r + f_c - 16 - u)

@@ -8,7 +8,7 @@ namespace tq {
 
 constexpr int OZ_M = 128;        // output rows per tile (A side, TMEM lanes)
 constexpr int OZ_N = 96;         // output columns per tile (B side)
-constexpr int OZ_CHUNK = 15;     // k-steps of 16 per exact flush (K = 240)
+constexpr int OZ_CHUNK = 21;     // most k-steps of 16 an accumulator holds (K = 336)
 constexpr int OZ_MAXS = 7;       // most slices supported
 constexpr int OZ_MAX_STAGES = 8;
 constexpr int OZ_EXP_ZERO = -(1 << 20);  // exponent of an all-zero row
