@@ -2,7 +2,8 @@
 FP64 oracle.  Block metadata is bit-exact with the native path; values are
 held to the stated error bound, written here as max|C - C_oracle| / max|C_oracle|:
     ozaki, 5 slices  <= 1e-10   (FP64-level target)
-    ozaki, 6 slices  <= 1e-12
+    ozaki, 6-7 slices <= 1e-11  (slice products with t+u >= 3 are accumulated
+                                 in rounded fp32, which floors the error near 1e-12)
     bf16x3 (3 slices) <= 1e-6   (FP32-level)"""
 import numpy as np
 import pytest
@@ -26,8 +27,8 @@ def rel_err(got, want):
     return float(np.max(np.abs(got - want)) / max(np.max(np.abs(want)), 1e-300))
 
 
-@pytest.mark.parametrize("precision,slices,tol", [("ozaki", 5, 1e-10), ("ozaki", 6, 1e-12),
-                                                  ("ozaki", 7, 1e-13), ("bf16x3", 3, 1e-6)])
+@pytest.mark.parametrize("precision,slices,tol", [("ozaki", 5, 1e-10), ("ozaki", 6, 1e-11),
+                                                  ("ozaki", 7, 1e-11), ("bf16x3", 3, 1e-6)])
 def test_small_u1_reference_layout(tq, precision, slices, tol):
     c = workloads.small_u1()
     A, B, hA, hB = gpu_pair(tq, c)
