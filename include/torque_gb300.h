@@ -69,6 +69,11 @@ typedef struct {
   int32_t precision; /* tq_precision */
   int32_t layout;    /* tq_layout */
   int32_t slices;    /* Ozaki slice count (0 = default); ignored otherwise */
+  int32_t tile_n;    /* tensor-core forms: output columns per tile, 32, 64 or 96
+                        (0 = 96); ignored otherwise */
+  int32_t native_fill; /* tensor-core forms, block grouping: output blocks whose
+                          tensor-core tiles are filled to less than
+                          native_fill / 1000 run in plain FP64 instead (0 = none) */
   int32_t reserved;
 } tq_contract_opts;
 
@@ -194,6 +199,63 @@ tq_status tq_plan_last_timings(tq_plan *plan, float *prepare_ms, float *gemm_ms)
  * (synchronises the stream): TQ_OK or TQ_ERR_TIMEOUT. */
 tq_status tq_plan_check(tq_plan *plan, tq_stream stream);
 tq_status tq_plan_destroy(tq_plan *plan);
+/* A new schedule (precision, slices, tile_n, native_fill; the layout stays)
+ * for a planned contraction, keeping its symbolic stage.  A plan created for
+ * plain arithmetic in the reference layout cannot take a tensor-core schedule
+ * (TQ_ERR_INVALID).  Synchronises the stream.  No reference counterpart. */
+tq_status tq_plan_reschedule(tq_plan *plan, const tq_contract_opts *opts, tq_stream stream);
+
+/* ---- schedule autotuning and the learned cost model ------------------- */
+/* No reference counterpart: the reference runs one fixed cuBLAS path
+ * (block_sparse.cuh:870-930). */
+
+#define TQ_N_FEATURES 32
+
+typedef struct {
+  tq_contract_opts opts; /* the candidate schedule (layout: the plan's) */
+  int32_t status;        /* TQ_OK, or why the candidate could not run */
+  float ms;              /* numeric stage, fastest of the timed runs (CUDA events) */
+  double rel_err;        /* max|C - C_fp64| / max|C_fp64| over the result */
+} tq_tune_entry;
+
+/* Exhaustive autotuner: runs every candidate schedule on the plan (one
+ * warm-up, then `reps` timed runs), measures its error against the plain FP64
+ * result of the same plan, and sets *best to the fastest candidate whose error
+ * is at most target_rel_err (-1: none).  The plan is left with the winner's
+ * schedule (its own if none).  Synchronises; float64 tensors only. */
+tq_status tq_autotune(tq_plan *plan, double target_rel_err, tq_tune_entry *cands,
+                      int32_t n_cands, int32_t reps, int32_t *best, tq_stream stream);
+
+/* The cost model's input: TQ_N_FEATURES floats describing the planned
+ * contraction and the target accuracy (-log10(target)/16, ranks, contracted
+ * legs and dimension, log flops, pairs and output blocks, and flop-weighted
+ * histograms of the block GEMM sizes m, n, k).  Synchronises. */
+tq_status tq_plan_features(const tq_plan *plan, double target_rel_err, float *features,
+                           tq_stream stream);
+
+/* A 3-layer FP32 perceptron (n_in -> width -> width -> n_out, ReLU), trained
+ * and evaluated on the device by the library's own kernels.  Inputs, outputs
+ * and targets are device arrays, row-major, one row per sample. */
+typedef struct tq_mlp tq_mlp;
+tq_status tq_mlp_create(int32_t n_in, int32_t width, int32_t n_out, uint64_t seed, tq_mlp **out);
+tq_status tq_mlp_destroy(tq_mlp *mlp);
+tq_status tq_mlp_num_params(const tq_mlp *mlp, int64_t *n_params);
+/* Parameters as W1[width][n_in] b1 W2[width][width] b2 W3[n_out][width] b3. */
+tq_status tq_mlp_get_params(tq_mlp *mlp, float *host);
+tq_status tq_mlp_set_params(tq_mlp *mlp, const float *host);
+/* Y (n x n_out, device) = network(X (n x n_in, device)). */
+tq_status tq_mlp_forward(tq_mlp *mlp, const float *X, int64_t n, float *Y, tq_stream stream);
+/* Loss (mean over samples and outputs of mask * (Y - T)^2, mask NULL = all
+ * ones) and its gradient with respect to every parameter, copied to the host
+ * (either pointer may be NULL).  Synchronises. */
+tq_status tq_mlp_gradients(tq_mlp *mlp, const float *X, const float *T, const float *mask,
+                           int64_t n, float *grads_host, float *loss_host, tq_stream stream);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) on the masked mean squared error
+ * of a batch; the batch loss goes to loss_dev (device, may be NULL).  No host
+ * synchronisation; the activation buffers grow on the first call with a larger
+ * batch. */
+tq_status tq_mlp_train_step(tq_mlp *mlp, const float *X, const float *T, const float *mask,
+                            int64_t n, float lr, float *loss_dev, tq_stream stream);
 
 /* ---- batches: many contractions in one launch -------------------------- */
 

@@ -27,8 +27,16 @@ ST = ctypes.c_int
 
 
 class ContractOpts(ctypes.Structure):
-    _fields_ = [("precision", I32), ("layout", I32), ("slices", I32), ("reserved", I32)]
+    _fields_ = [("precision", I32), ("layout", I32), ("slices", I32), ("tile_n", I32),
+                ("native_fill", I32), ("reserved", I32)]
 
+
+class TuneEntry(ctypes.Structure):
+    _fields_ = [("opts", ContractOpts), ("status", I32), ("ms", ctypes.c_float),
+                ("rel_err", ctypes.c_double)]
+
+
+TQ_N_FEATURES = 32
 
 SIGNATURES = {
     "tq_bs_create_empty": (ST, [I32, I32, P64, PP]),
@@ -56,6 +64,17 @@ SIGNATURES = {
     "tq_plan_last_timings": (ST, [P, ctypes.POINTER(ctypes.c_float),
                                   ctypes.POINTER(ctypes.c_float)]),
     "tq_plan_check": (ST, [P, P]),
+    "tq_plan_reschedule": (ST, [P, ctypes.POINTER(ContractOpts), P]),
+    "tq_plan_features": (ST, [P, ctypes.c_double, ctypes.POINTER(ctypes.c_float), P]),
+    "tq_autotune": (ST, [P, ctypes.c_double, P, I32, I32, ctypes.POINTER(I32), P]),
+    "tq_mlp_create": (ST, [I32, I32, I32, ctypes.c_uint64, PP]),
+    "tq_mlp_destroy": (ST, [P]),
+    "tq_mlp_num_params": (ST, [P, P64]),
+    "tq_mlp_get_params": (ST, [P, P]),
+    "tq_mlp_set_params": (ST, [P, P]),
+    "tq_mlp_forward": (ST, [P, P, I64, P, P]),
+    "tq_mlp_gradients": (ST, [P, P, P, P, I64, P, P, P]),
+    "tq_mlp_train_step": (ST, [P, P, P, P, I64, ctypes.c_float, P, P]),
     "tq_batch_create": (ST, [PP, I32, ctypes.POINTER(I32), P, PP]),
     "tq_batch_execute": (ST, [P, P]),
     "tq_batch_graph_launch": (ST, [P, P]),

@@ -219,12 +219,14 @@ class BlockSparseTensor:
 
     # ------------------------------------------------------------ operations
     def contract(self, tensor: "BlockSparseTensor", contracting_indices, precision="native",
-                 layout="reference", slices=0, stream=None) -> "BlockSparseTensor":
+                 layout="reference", slices=0, tile_n=0, native_fill=0,
+                 stream=None) -> "BlockSparseTensor":
         """Contract legs contracting_indices[k][0] of self with [k][1] of tensor
-        (an n x 2 matrix, as in the reference)."""
+        (an n x 2 matrix, as in the reference).  precision, slices, tile_n and
+        native_fill are the schedule (tq_contract_opts)."""
         ci = np.asarray(contracting_indices, dtype=np.int64).reshape(-1, 2)
         al, bl = _i64(ci[:, 0]), _i64(ci[:, 1])
-        opts = ContractOpts(_lib.PRECISIONS[precision], _lib.LAYOUTS[layout], slices, 0)
+        opts = make_opts(precision, layout, slices, tile_n, native_fill)
         h = ctypes.c_void_p()
         check(load().tq_bs_contract(self._h, tensor._h, ci.shape[0], _p64(al), _p64(bl),
                                     ctypes.byref(opts), _stream(stream), ctypes.byref(h)))
@@ -251,15 +253,25 @@ class BlockSparseTensor:
         return BlockSparseTensor(_handle=h)
 
 
+def make_opts(precision="native", layout="reference", slices=0, tile_n=0, native_fill=0):
+    """tq_contract_opts from names: precision native|ozaki|bf16x3, layout
+    reference|reduced; slices, tile_n (32/64/96) and native_fill (per mille)
+    apply to the tensor-core forms."""
+    return ContractOpts(_lib.PRECISIONS[precision], _lib.LAYOUTS[layout], int(slices), int(tile_n),
+                        int(native_fill), 0)
+
+
 class ContractionPlan:
     """The symbolic stage of a contraction, kept for repeated numeric runs
     (tq_plan_create / tq_plan_execute)."""
 
     def __init__(self, A: BlockSparseTensor, B: BlockSparseTensor, contracting_indices,
-                 precision="native", layout="reference", slices=0, stream=None):
+                 precision="native", layout="reference", slices=0, tile_n=0, native_fill=0,
+                 stream=None):
         ci = np.asarray(contracting_indices, dtype=np.int64).reshape(-1, 2)
         al, bl = _i64(ci[:, 0]), _i64(ci[:, 1])
-        opts = ContractOpts(_lib.PRECISIONS[precision], _lib.LAYOUTS[layout], slices, 0)
+        opts = make_opts(precision, layout, slices, tile_n, native_fill)
+        self.layout = opts.layout
         self._p = ctypes.c_void_p()
         h = ctypes.c_void_p()
         self.A, self.B = A, B  # keep the operands alive
@@ -300,6 +312,34 @@ class ContractionPlan:
         n = ctypes.c_int64()
         check(load().tq_plan_flops(self._p, ctypes.byref(f), ctypes.byref(n)))
         return n.value
+
+    def reschedule(self, precision="native", slices=0, tile_n=0, native_fill=0, stream=None):
+        """A new schedule for this plan (tq_plan_reschedule); the layout stays."""
+        o = make_opts(precision, "reference", slices, tile_n, native_fill)
+        o.layout = self.layout
+        check(load().tq_plan_reschedule(self._p, ctypes.byref(o), _stream(stream)))
+
+    def features(self, target_rel_err: float, stream=None) -> np.ndarray:
+        """The cost model's TQ_N_FEATURES inputs for this contraction (tq_plan_features)."""
+        f = (ctypes.c_float * _lib.TQ_N_FEATURES)()
+        check(load().tq_plan_features(self._p, float(target_rel_err), f, _stream(stream)))
+        return np.ctypeslib.as_array(f).copy()
+
+    def autotune(self, target_rel_err: float, candidates, reps: int = 3, stream=None):
+        """Exhaustive autotuning (tq_autotune) over candidate schedules, each a
+        dict of make_opts keywords.  Returns (best index or -1, [(status, ms,
+        rel_err)]); the plan keeps the winner's schedule."""
+        n = len(candidates)
+        arr = (_lib.TuneEntry * max(n, 1))()
+        for i, c in enumerate(candidates):
+            o = make_opts(c.get("precision", "native"), "reference", c.get("slices", 0),
+                          c.get("tile_n", 0), c.get("native_fill", 0))
+            o.layout = self.layout
+            arr[i].opts = o
+        best = ctypes.c_int32()
+        check(load().tq_autotune(self._p, float(target_rel_err), arr, n, int(reps),
+                                 ctypes.byref(best), _stream(stream)))
+        return best.value, [(arr[i].status, arr[i].ms, arr[i].rel_err) for i in range(n)]
 
     def __del__(self):
         p = getattr(self, "_p", None)

@@ -16,8 +16,9 @@ using namespace tq;
 
 struct tq_batch {
   struct Wave {
-    OzBatchDev oz;                 // the tensor-core plans of the wave, as one launch
-    bool has_oz = false;
+    // the tensor-core plans of the wave: one launch per tile width in use
+    std::vector<std::unique_ptr<OzBatchDev>> oz;
+    std::vector<tq_plan *> hybrid;  // of those, plans with blocks grouped to plain FP64
     std::vector<tq_plan *> others;  // native-precision, rank-0 or empty plans
   };
   std::vector<std::unique_ptr<Wave>> waves;
@@ -35,10 +36,11 @@ struct tq_batch {
 
 static tq_status batch_run(tq_batch *b, cudaStream_t s) {
   for (auto &w : b->waves) {
-    if (w->has_oz) {
-      TQ_CHECK(oz_batch_prepare(w->oz, s));
-      TQ_CHECK(oz_batch_gemm(w->oz, s));
+    for (auto &oz : w->oz) {
+      TQ_CHECK(oz_batch_prepare(*oz, s));
+      TQ_CHECK(oz_batch_gemm(*oz, s));
     }
+    for (tq_plan *P : w->hybrid) TQ_CHECK(run_hybrid_native(P, s));
     for (tq_plan *P : w->others) TQ_CHECK(plan_run(P, s));
   }
   return TQ_OK;
@@ -52,6 +54,7 @@ tq_status tq_batch_create(tq_plan *const *plans, int32_t n, const int32_t *wave,
   if (n < 0) return fail(TQ_ERR_INVALID, "negative plan count");
   for (int32_t i = 0; i < n; i++) {
     if (!plans[i]) return fail(TQ_ERR_INVALID, "plan is NULL");
+    if (!plans[i]->sched_ok) return fail(TQ_ERR_INVALID, "a plan's last reschedule failed");
     if (wave && i && wave[i] < wave[i - 1])
       return fail(TQ_ERR_INVALID, "waves must be non-decreasing");
   }
@@ -62,21 +65,25 @@ tq_status tq_batch_create(tq_plan *const *plans, int32_t n, const int32_t *wave,
   while (i < n) {
     const int32_t wv = wave ? wave[i] : 0;
     std::unique_ptr<tq_batch::Wave> w(new tq_batch::Wave());
-    std::vector<OzJob> jobs;
-    std::vector<OzSide> sides;
+    std::vector<OzJob> jobs[3];
+    std::vector<OzSide> sides[3];
     for (; i < n && (wave ? wave[i] : 0) == wv; i++) {
       tq_plan *P = plans[i];
       if (P->tc && P->C->rank > 0 && P->tc_tiles > 0) {
-        jobs.push_back(P->tc_job);
-        sides.push_back(P->tc_side[0]);
-        sides.push_back(P->tc_side[1]);
+        const int k = P->tile_n == 32 ? 0 : P->tile_n == 64 ? 1 : 2;
+        jobs[k].push_back(P->tc_job);
+        sides[k].push_back(P->tc_side[0]);
+        sides[k].push_back(P->tc_side[1]);
+        if (P->hyb_tiles) w->hybrid.push_back(P);
       } else {
         w->others.push_back(P);
       }
     }
-    if (!jobs.empty()) {
-      TQ_CHECK(oz_batch_build(jobs, sides, s, w->oz));
-      w->has_oz = true;
+    for (int k = 0; k < 3; k++) {
+      if (jobs[k].empty()) continue;
+      std::unique_ptr<OzBatchDev> oz(new OzBatchDev());
+      TQ_CHECK(oz_batch_build(jobs[k], sides[k], s, *oz));
+      w->oz.push_back(std::move(oz));
     }
     b->waves.push_back(std::move(w));
   }
@@ -120,7 +127,7 @@ tq_status tq_batch_check(tq_batch *b, tq_stream stream) {
   cudaStream_t s = (cudaStream_t)stream;
   TQ_CUDA(cudaStreamSynchronize(s));
   for (auto &w : b->waves) {
-    if (w->has_oz) TQ_CHECK(oz_batch_check(w->oz, s));
+    for (auto &oz : w->oz) TQ_CHECK(oz_batch_check(*oz, s));
     for (tq_plan *P : w->others) TQ_CHECK(plan_check(P, s));
   }
   return TQ_OK;

@@ -223,9 +223,14 @@ __global__ void tc_block_stats_kernel(OzSide S, int32_t rt_rows, int32_t slices,
   mkey[S.key[b]] = m;
 }
 
+// Per output block: k-steps of its pairs and its tensor-core tiles; with block
+// grouping, outputs whose tiles would be filled to less than native_fill/1000
+// get no tensor-core tiles and their native tiles (nt_native, the 64x64 tiling
+// of the native kernel) instead.
 __global__ void tc_out_kernel(DevBS A, DevBS B, LegSpec L, const int32_t *pa, const int32_t *pb,
                               const int64_t *seg, const int64_t *perm, int64_t n_out,
-                              int32_t *nk_pair, int64_t *tiles, int64_t *ksum) {
+                              int32_t tile_n, int32_t native_fill, int32_t *nk_pair,
+                              int64_t *tiles, int64_t *ksum, int64_t *nt_native) {
   const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= n_out) return;
   int64_t tot = 0;
@@ -245,7 +250,87 @@ __global__ void tc_out_kernel(DevBS A, DevBS B, LegSpec L, const int32_t *pa, co
     m *= A.end[pa[p0] * A.rank + L.fa[q]] - A.begin[pa[p0] * A.rank + L.fa[q]] + 1;
   for (int q = 0; q < L.nfb; q++)
     n *= B.end[pb[p0] * B.rank + L.fb[q]] - B.begin[pb[p0] * B.rank + L.fb[q]] + 1;
-  tiles[o] = ((m + OZ_M - 1) / OZ_M) * ((n + OZ_N - 1) / OZ_N);
+  const int64_t t = ((m + OZ_M - 1) / OZ_M) * ((n + tile_n - 1) / tile_n);
+  // fill = m n / (t OZ_M tile_n) < native_fill / 1000
+  const bool native = m * n * 1000 < (int64_t)native_fill * t * OZ_M * tile_n;
+  tiles[o] = native ? 0 : t;
+  nt_native[o] = native ? ((m + NT_TM - 1) / NT_TM) * ((n + NT_TN - 1) / NT_TN) : 0;
+}
+
+// Split-K of the native kernel: per output its fused K, K chunks per tile
+// (at most S, chunks of at least kmin columns), work items, reduced tiles and
+// partial-tile slots.
+__global__ void native_work_kernel(DevBS A, DevBS B, LegSpec L, const int32_t *pa,
+                                   const int32_t *pb, const int64_t *seg, const int64_t *perm,
+                                   int64_t n_out, const int64_t *tiles, int32_t S, int64_t kmin,
+                                   int32_t *chunks, int64_t *kfused, int64_t *work,
+                                   int64_t *nsplit, int64_t *slots) {
+  const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= n_out) return;
+  int64_t kf = 0;
+  for (int64_t sidx = seg[o]; sidx < seg[o + 1]; sidx++) {
+    const int64_t p = perm ? perm[sidx] : sidx;
+    int64_t cb[TQ_MAXR], ce[TQ_MAXR], k = 1;
+    contraction_range(A, B, L, pa[p], pb[p], cb, ce);
+    for (int c = 0; c < L.nc; c++) k *= ce[c] - cb[c] + 1;
+    kf += k;
+  }
+  int64_t ch = tiles[o] > 0 ? kf / kmin : 1;
+  ch = ch < 1 ? 1 : (ch > S ? S : ch);
+  chunks[o] = (int32_t)ch;
+  kfused[o] = kf;
+  work[o] = tiles[o] * ch;
+  nsplit[o] = ch > 1 ? tiles[o] : 0;
+  slots[o] = ch > 1 ? tiles[o] * ch : 0;
+}
+
+// The native launch over `total` tiles (tiles[o] per output, tile_start their
+// exclusive scan): without split-K when the tiles alone give every SM about 8
+// CTAs; otherwise each tile is cut into up to S K chunks.
+static tq_status native_work(const tq_plan *P, const int64_t *tiles, const int64_t *tile_start,
+                             int64_t total, NativeWorkDev &W, cudaStream_t s) {
+  W.w = NativeWork{};
+  W.w.n_work = total;
+  W.w.work_start = tile_start;
+  if (total == 0 || P->n_out == 0) return TQ_OK;
+  int dev = 0, sms = 0;
+  TQ_CUDA(cudaGetDevice(&dev));
+  TQ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t target = 8 * (int64_t)sms;
+  if (total >= target) return TQ_OK;
+  const int32_t S = (int32_t)std::min<int64_t>(32, (target + total - 1) / total);
+  const int64_t no = P->n_out;
+  DevArray<int64_t> work, nsplit, slots, tot;
+  TQ_CHECK(W.chunks.alloc(no, s));
+  TQ_CHECK(W.kfused.alloc(no, s));
+  TQ_CHECK(W.work_start.alloc(no, s));
+  TQ_CHECK(W.split_start.alloc(no, s));
+  TQ_CHECK(W.split_off.alloc(no, s));
+  TQ_CHECK(work.alloc(no, s));
+  TQ_CHECK(nsplit.alloc(no, s));
+  TQ_CHECK(slots.alloc(no, s));
+  TQ_CHECK(tot.alloc(3, s));
+  count_launch(), native_work_kernel<<<nblk(no), 256, 0, s>>>(
+      P->A->view(), P->B->view(), P->L, P->pa.p, P->pb.p, P->seg.p, P->perm.p, no, tiles, S,
+      (int64_t)256, W.chunks.p, W.kfused.p, work.p, nsplit.p, slots.p);
+  TQ_CUDA(cudaGetLastError());
+  TQ_CHECK(scan_exclusive(work.p, W.work_start.p, no, tot.p, s));
+  TQ_CHECK(scan_exclusive(nsplit.p, W.split_start.p, no, tot.p + 1, s));
+  TQ_CHECK(scan_exclusive(slots.p, W.split_off.p, no, tot.p + 2, s));
+  int64_t h[3];
+  TQ_CUDA(cudaMemcpyAsync(h, tot.p, 24, cudaMemcpyDeviceToHost, s));
+  TQ_CUDA(cudaStreamSynchronize(s));
+  if (h[1] == 0) return TQ_OK;  // nothing long enough to split
+  TQ_CHECK(W.scratch.alloc((size_t)h[2] * NT_TM * NT_TN * dtype_size(P->A->dtype), s));
+  W.w.n_work = h[0];
+  W.w.n_split = h[1];
+  W.w.work_start = W.work_start.p;
+  W.w.split_start = W.split_start.p;
+  W.w.split_off = W.split_off.p;
+  W.w.chunks = W.chunks.p;
+  W.w.kfused = W.kfused.p;
+  W.w.scratch = W.scratch.p;
+  return TQ_OK;
 }
 
 GemmJob make_gemm_job(const tq_plan *P) {
@@ -261,6 +346,10 @@ GemmJob make_gemm_job(const tq_plan *P) {
   job.c_off = P->C->d_meta.p ? P->C->d_meta.p + 3 * P->n_out * P->C->rank : nullptr;
   job.C = P->C->data;
   job.n_out = P->n_out;
+  job.chunks = nullptr;
+  job.kfused = nullptr;
+  job.split_off = nullptr;
+  job.scratch = nullptr;
   return job;
 }
 
@@ -290,6 +379,11 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   if (sl == 0) sl = P->opts.precision == TQ_PREC_OZAKI ? 5 : 3;
   if (sl < 1 || sl > OZ_MAXS) return fail(TQ_ERR_INVALID, "slice count outside 1..7");
   P->slices = sl;
+  const int32_t tn = P->opts.tile_n ? P->opts.tile_n : OZ_N;
+  if (tn != 32 && tn != 64 && tn != 96) return fail(TQ_ERR_INVALID, "tile width must be 32, 64 or 96");
+  if (P->opts.native_fill < 0 || P->opts.native_fill > 1000)
+    return fail(TQ_ERR_INVALID, "native_fill outside 0..1000");
+  P->tile_n = tn;
   if (KA > (1 << 26) || KB > (1 << 26))
     return fail(TQ_ERR_UNSUPPORTED, "too many distinct free boxes for the sliced forms");
   const int64_t np = P->n_pairs, no = P->n_out;
@@ -314,7 +408,7 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   OzSide SA = make_side(A, L.nfa, L.fa, L.nc, L.al, P->keyA.p, nullptr, nullptr, nullptr, nullptr);
   OzSide SB = make_side(B, L.nfb, L.fb, L.nc, L.bl, P->keyB.p, nullptr, nullptr, nullptr, nullptr);
   count_launch(), tc_block_stats_kernel<<<nblk(A->nb), 256, 0, s>>>(SA, OZ_M, sl, mkA.p, rA.p, tA.p, uA.p);
-  count_launch(), tc_block_stats_kernel<<<nblk(B->nb), 256, 0, s>>>(SB, OZ_N, sl, mkB.p, rB.p, tB.p, uB.p);
+  count_launch(), tc_block_stats_kernel<<<nblk(B->nb), 256, 0, s>>>(SB, tn, sl, mkB.p, rB.p, tB.p, uB.p);
   TQ_CUDA(cudaGetLastError());
   TQ_CHECK(P->rowstartA.alloc(A->nb, s));
   TQ_CHECK(P->tilestartA.alloc(A->nb, s));
@@ -337,13 +431,18 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   TQ_CHECK(P->ksum.alloc(no, s));
   TQ_CHECK(tiles.alloc(no, s));
   TQ_CHECK(P->tc_tile_start.alloc(no + 1, s));
+  DevArray<int64_t> nt_native;
+  TQ_CHECK(nt_native.alloc(no, s));
+  TQ_CHECK(P->hyb_tile_start.alloc(no + 1, s));
   count_launch(), tc_out_kernel<<<nblk(no), 256, 0, s>>>(A->view(), B->view(), L, P->pa.p, P->pb.p, P->seg.p,
-                                          P->perm.p, no, P->nk_pair.p, tiles.p, P->ksum.p);
+                                          P->perm.p, no, tn, P->opts.native_fill,
+                                          P->nk_pair.p, tiles.p, P->ksum.p, nt_native.p);
   TQ_CUDA(cudaGetLastError());
   TQ_CHECK(scan_exclusive(tiles.p, P->tc_tile_start.p, no, tot.p + 8, s));
+  TQ_CHECK(scan_exclusive(nt_native.p, P->hyb_tile_start.p, no, tot.p + 9, s));
   int64_t h[10];
   int32_t h_bad = 0;
-  TQ_CUDA(cudaMemcpyAsync(h, tot.p, 9 * 8, cudaMemcpyDeviceToHost, s));
+  TQ_CUDA(cudaMemcpyAsync(h, tot.p, 10 * 8, cudaMemcpyDeviceToHost, s));
   TQ_CUDA(cudaMemcpyAsync(&h_bad, bad.p, 4, cudaMemcpyDeviceToHost, s));
   TQ_CUDA(cudaStreamSynchronize(s));
   if (h_bad)
@@ -357,6 +456,10 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   P->tilesB = h[5];
   P->nexpB = h[7];
   P->tc_tiles = h[8];
+  P->hyb_tiles = h[9];
+  if (P->hyb_tiles < 0 || P->hyb_tiles > P->n_tiles)
+    return fail(TQ_ERR_CUDA, "inconsistent block grouping (native tiles above the plan's)");
+  TQ_CHECK(native_work(P, nt_native.p, P->hyb_tile_start.p, P->hyb_tiles, P->hyb, s));
   TQ_CHECK(P->expA.alloc(std::max<int64_t>(P->nexpA, 1), s));
   TQ_CHECK(P->expB.alloc(std::max<int64_t>(P->nexpB, 1), s));
   TQ_CHECK(P->sliceA.alloc(std::max<int64_t>(h[2], 1) * 256, s));
@@ -378,7 +481,7 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
     S.n_tiles = n_tiles[k];
     S.n_exps = n_exps[k];
     S.s = sl;
-    S.rt_rows = k == 0 ? OZ_M : OZ_N;
+    S.rt_rows = k == 0 ? OZ_M : tn;
   }
   OzJob &J = P->tc_job;
   J.g = make_gemm_job(P);
@@ -397,13 +500,24 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   J.expA = P->expA.p;
   J.expB = P->expB.p;
   J.s = sl;
+  J.tile_n = tn;
   return oz_batch_build({J}, {P->tc_side[0], P->tc_side[1]}, s, P->tcb);
 }
 
+// The output blocks that block grouping sent to plain FP64 (after the sliced
+// launch; the two write disjoint output blocks).
+tq_status run_hybrid_native(tq_plan *P, cudaStream_t s) {
+  if (!P->tc || P->hyb_tiles == 0) return TQ_OK;
+  GemmJob job = make_gemm_job(P);
+  job.tile_start = P->hyb_tile_start.p;
+  return launch_gemm_native(job, P->hyb_tiles, P->A->dtype, s, &P->hyb.w);
+}
+
 static tq_status run_tc(tq_plan *P, cudaStream_t s) {
-  TQ_CHECK(oz_batch_prepare(P->tcb, s));
+  if (P->tc_tiles) TQ_CHECK(oz_batch_prepare(P->tcb, s));
   if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[1], s));
-  return oz_batch_gemm(P->tcb, s);
+  if (P->tc_tiles) TQ_CHECK(oz_batch_gemm(P->tcb, s));
+  return run_hybrid_native(P, s);
 }
 
 tq_status validate_legs(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,
@@ -440,7 +554,7 @@ tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64
                      tq_plan **plan_out, tq_bs **out) {
   LegSpec L;
   TQ_CHECK(validate_legs(A, B, n_legs, a_legs, b_legs, L));
-  tq_contract_opts o = {TQ_PREC_NATIVE, TQ_LAYOUT_REFERENCE, 0, 0};
+  tq_contract_opts o = {TQ_PREC_NATIVE, TQ_LAYOUT_REFERENCE, 0, 0, 0, 0};
   if (opts) o = *opts;
   if (o.precision != TQ_PREC_NATIVE && o.precision != TQ_PREC_OZAKI &&
       o.precision != TQ_PREC_BF16X3)
@@ -575,8 +689,12 @@ tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64
     P->flops = 2.0 * (double)h[1];
     P->n_tiles = h[3];
     TQ_CHECK(alloc_data(C, h[2], s));
+    TQ_CHECK(native_work(P.get(), tiles.p, P->tile_start.p, P->n_tiles, P->nat, s));
     C->host_valid = false;
     C->dev_valid = true;
+    P->KA = KA;
+    P->KB = KB;
+    P->keys = (o.layout == TQ_LAYOUT_REDUCED || P->tc) && n_pairs;
     if (P->tc && n_pairs) TQ_CHECK(plan_tc(P.get(), KA, KB, s));
   }
   P->C = C;
@@ -586,7 +704,34 @@ tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64
   return TQ_OK;
 }
 
+// A new schedule (precision, slices, tile width, grouping) for a planned
+// contraction: the symbolic stage is kept, only the tensor-core part is rebuilt.
+tq_status plan_reschedule(tq_plan *P, const tq_contract_opts &o, cudaStream_t s) {
+  if (o.precision != TQ_PREC_NATIVE && o.precision != TQ_PREC_OZAKI &&
+      o.precision != TQ_PREC_BF16X3)
+    return fail(TQ_ERR_INVALID, "unknown precision");
+  if (o.layout != P->opts.layout) return fail(TQ_ERR_INVALID, "a new schedule keeps the layout");
+  if (o.precision != TQ_PREC_NATIVE && P->A->dtype != TQ_F64)
+    return fail(TQ_ERR_UNSUPPORTED, "tensor-core forms take float64 tensors");
+  const bool tc = o.precision != TQ_PREC_NATIVE && P->C->rank > 0 && P->n_pairs > 0;
+  if (tc && !P->keys)
+    return fail(TQ_ERR_INVALID,
+                "plan was made for plain arithmetic in the reference layout; create it with a "
+                "tensor-core precision or the reduced layout to reschedule it");
+  // wait for launches that still read the old schedule's arrays
+  TQ_CUDA(cudaStreamSynchronize(s));
+  P->opts = o;
+  P->tc = o.precision != TQ_PREC_NATIVE;
+  P->tc_tiles = P->hyb_tiles = 0;
+  P->sched_ok = false;
+  if (tc) TQ_CHECK(plan_tc(P, P->KA, P->KB, s));
+  P->sched_ok = true;
+  return TQ_OK;
+}
+
 tq_status plan_run(tq_plan *P, cudaStream_t s) {
+  if (!P->sched_ok)
+    return fail(TQ_ERR_INVALID, "the plan's last reschedule failed; give it a valid schedule");
   const GemmJob job = make_gemm_job(P);
   if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[0], s));
   tq_status st = TQ_OK;
@@ -598,7 +743,7 @@ tq_status plan_run(tq_plan *P, cudaStream_t s) {
     st = run_tc(P, s);
   } else {
     if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[1], s));
-    if (P->n_tiles) st = launch_gemm_native(job, P->n_tiles, P->A->dtype, s);
+    if (P->n_tiles) st = launch_gemm_native(job, P->n_tiles, P->A->dtype, s, &P->nat.w);
   }
   if (st == TQ_OK && P->profile) TQ_CUDA(cudaEventRecord(P->ev[2], s));
   return st;
@@ -625,6 +770,11 @@ tq_status tq_plan_create(const tq_bs *A, const tq_bs *B, int32_t n_legs, const i
 tq_status tq_plan_execute(tq_plan *plan, tq_stream stream) {
   if (!plan) return fail(TQ_ERR_INVALID, "plan is NULL");
   return plan_run(plan, (cudaStream_t)stream);
+}
+
+tq_status tq_plan_reschedule(tq_plan *plan, const tq_contract_opts *opts, tq_stream stream) {
+  if (!plan || !opts) return fail(TQ_ERR_INVALID, "NULL argument");
+  return plan_reschedule(plan, *opts, (cudaStream_t)stream);
 }
 
 tq_status tq_plan_flops(const tq_plan *plan, double *flops, int64_t *n_pairs) {

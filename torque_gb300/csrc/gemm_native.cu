@@ -22,7 +22,8 @@ __device__ __forceinline__ int64_t find_seg(const int64_t *start, int64_t n, int
 
 template <typename T>
 __device__ __forceinline__ void load_tile(const T *__restrict__ data, const Operand &op,
-                                          int64_t r0, int64_t k0, T (*S)[NT_TM + 1]) {
+                                          int64_t r0, int64_t k0, int64_t kmax,
+                                          T (*S)[NT_TM + 1]) {
   const int64_t rs = row_stride(op), cs = col_stride(op);
   const int t = threadIdx.x;
   const bool m_major = rs == 1 || (rs != -1 && cs != 1);
@@ -34,7 +35,7 @@ __device__ __forceinline__ void load_tile(const T *__restrict__ data, const Oper
     else { kk = e % NT_TK; r = e / NT_TK; }
     const int64_t gr = r0 + r, gk = k0 + kk;
     T v = T(0);
-    if (gr < op.rows && gk < op.cols) {
+    if (gr < op.rows && gk < kmax) {
       int64_t a;
       if (rs >= 0 && cs >= 0) a = op.base + gr * rs + gk * cs;
       else a = op.base + mixed_addr(gr, op.nr, op.rdim, op.rst) + mixed_addr(gk, op.nc, op.cdim, op.cst);
@@ -44,32 +45,56 @@ __device__ __forceinline__ void load_tile(const T *__restrict__ data, const Oper
   }
 }
 
+// Rows and columns of output o (from its first pair).
+__device__ __forceinline__ void out_dims(const GemmJob &job, int64_t o, int64_t &m, int64_t &n) {
+  const int64_t p0 = job.perm ? job.perm[job.seg[o]] : job.seg[o];
+  const int64_t i = job.pa[p0], j = job.pb[p0];
+  m = 1;
+  n = 1;
+  for (int q = 0; q < job.L.nfa; q++)
+    m *= job.A.end[i * job.A.rank + job.L.fa[q]] - job.A.begin[i * job.A.rank + job.L.fa[q]] + 1;
+  for (int q = 0; q < job.L.nfb; q++)
+    n *= job.B.end[j * job.B.rank + job.L.fb[q]] - job.B.begin[j * job.B.rank + job.L.fb[q]] + 1;
+}
+
+// One CTA per work item: an output tile, or one K chunk of it (split-K).  A
+// chunk covers a contiguous range of the output's fused K (its pairs' columns
+// back to back, in pair order); chunk boundaries fall on multiples of 16.
 template <typename T>
 __global__ void __launch_bounds__(NT_THREADS) gemm_native_kernel(GemmJob job, int64_t tile_base) {
   __shared__ T As[NT_TK][NT_TM + 1];
   __shared__ T Bs[NT_TK][NT_TN + 1];
   __shared__ Operand opA, opB;
-  __shared__ int64_t s_o, s_tm, s_tn;
+  __shared__ int64_t s_o, s_tm, s_tn, s_tile, s_klo, s_khi;
+  __shared__ int32_t s_c, s_ch;
   const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
   const int64_t tile = tile_base + blockIdx.x;
   if (t == 0) {
     const int64_t o = find_seg(job.tile_start, job.n_out, tile);
     s_o = o;
-    // rows/cols of the output block come from its first pair
-    const int64_t p0 = job.perm ? job.perm[job.seg[o]] : job.seg[o];
-    const int64_t i = job.pa[p0], j = job.pb[p0];
-    int64_t m = 1, n = 1;
-    for (int q = 0; q < job.L.nfa; q++)
-      m *= job.A.end[i * job.A.rank + job.L.fa[q]] - job.A.begin[i * job.A.rank + job.L.fa[q]] + 1;
-    for (int q = 0; q < job.L.nfb; q++)
-      n *= job.B.end[j * job.B.rank + job.L.fb[q]] - job.B.begin[j * job.B.rank + job.L.fb[q]] + 1;
+    int64_t m, n;
+    out_dims(job, o, m, n);
     const int64_t tiles_m = (m + NT_TM - 1) / NT_TM;
-    const int64_t local = tile - job.tile_start[o];
+    int64_t local = tile - job.tile_start[o];
+    const int32_t ch = job.chunks ? job.chunks[o] : 1;
+    const int32_t c = (int32_t)(local % ch);
+    local /= ch;
+    s_tile = local;
     s_tm = local % tiles_m;
     s_tn = local / tiles_m;
+    s_c = c;
+    s_ch = ch;
+    if (ch > 1) {
+      const int64_t kf = job.kfused[o];
+      s_klo = (kf * c / ch) & ~(int64_t)15;
+      s_khi = c + 1 == ch ? kf : (kf * (c + 1) / ch) & ~(int64_t)15;
+    } else {
+      s_klo = 0;
+      s_khi = INT64_MAX;
+    }
   }
   __syncthreads();
-  const int64_t o = s_o, r0 = s_tm * NT_TM, c0 = s_tn * NT_TN;
+  const int64_t o = s_o, r0 = s_tm * NT_TM, c0 = s_tn * NT_TN, klo = s_klo, khi = s_khi;
   const T *Ad = (const T *)job.A.data;
   const T *Bd = (const T *)job.B.data;
   T acc[4][4];
@@ -78,7 +103,8 @@ __global__ void __launch_bounds__(NT_THREADS) gemm_native_kernel(GemmJob job, in
 #pragma unroll
     for (int b = 0; b < 4; b++) acc[a][b] = T(0);
 
-  for (int64_t sidx = job.seg[o]; sidx < job.seg[o + 1]; sidx++) {
+  int64_t pos = 0;  // fused-K column of the current pair's first column
+  for (int64_t sidx = job.seg[o]; sidx < job.seg[o + 1] && pos < khi; sidx++) {
     const int64_t p = job.perm ? job.perm[sidx] : sidx;
     if (t == 0 || t == 32) {
       const int64_t i = job.pa[p], j = job.pb[p];
@@ -91,9 +117,11 @@ __global__ void __launch_bounds__(NT_THREADS) gemm_native_kernel(GemmJob job, in
     }
     __syncthreads();
     const int64_t K = opA.cols;
-    for (int64_t k0 = 0; k0 < K; k0 += NT_TK) {
-      load_tile<T>(Ad, opA, r0, k0, As);
-      load_tile<T>(Bd, opB, c0, k0, Bs);
+    const int64_t kb = klo > pos ? klo - pos : 0;
+    const int64_t ke = khi - pos < K ? khi - pos : K;
+    for (int64_t k0 = kb; k0 < ke; k0 += NT_TK) {
+      load_tile<T>(Ad, opA, r0, k0, ke, As);
+      load_tile<T>(Bd, opB, c0, k0, ke, Bs);
       __syncthreads();
 #pragma unroll
       for (int kk = 0; kk < NT_TK; kk++) {
@@ -110,8 +138,20 @@ __global__ void __launch_bounds__(NT_THREADS) gemm_native_kernel(GemmJob job, in
       }
       __syncthreads();
     }
+    pos += K;
+    __syncthreads();  // every thread has read opA.cols before the next pair's operands
   }
-  const int64_t m = opA.rows, n = opB.rows;
+  if (s_ch > 1) {
+    // partial tile, full 64x64, in chunk order after the tile's other chunks
+    T *P = (T *)job.scratch + (job.split_off[o] + s_tile * s_ch + s_c) * (int64_t)(NT_TM * NT_TN);
+#pragma unroll
+    for (int y = 0; y < 4; y++)
+#pragma unroll
+      for (int x = 0; x < 4; x++) P[(tx + 16 * x) + (ty + 16 * y) * NT_TM] = acc[x][y];
+    return;
+  }
+  int64_t m, n;
+  out_dims(job, o, m, n);
   T *C = (T *)job.C + job.c_off[o];
 #pragma unroll
   for (int y = 0; y < 4; y++) {
@@ -125,7 +165,41 @@ __global__ void __launch_bounds__(NT_THREADS) gemm_native_kernel(GemmJob job, in
   }
 }
 
-tq_status launch_gemm_native(const GemmJob &job, int64_t n_tiles, tq_dtype dt, cudaStream_t s) {
+// Split tiles: C tile = sum of its chunk partials in chunk order.
+template <typename T>
+__global__ void __launch_bounds__(NT_THREADS) split_reduce_kernel(GemmJob job,
+                                                                  const int64_t *split_start,
+                                                                  int64_t base) {
+  const int64_t st = base + blockIdx.x;
+  const int64_t o = find_seg(split_start, job.n_out, st);
+  const int64_t local = st - split_start[o];
+  int64_t m, n;
+  out_dims(job, o, m, n);
+  const int64_t tiles_m = (m + NT_TM - 1) / NT_TM;
+  const int64_t r0 = (local % tiles_m) * NT_TM, c0 = (local / tiles_m) * NT_TN;
+  const int ch = job.chunks[o];
+  const T *P = (const T *)job.scratch + (job.split_off[o] + local * ch) * (int64_t)(NT_TM * NT_TN);
+  T *C = (T *)job.C + job.c_off[o];
+  for (int e = threadIdx.x; e < NT_TM * NT_TN; e += NT_THREADS) {
+    const int64_t r = r0 + e % NT_TM, c = c0 + e / NT_TM;
+    if (r >= m || c >= n) continue;
+    T v = P[e];
+    for (int q = 1; q < ch; q++) v += P[(int64_t)q * NT_TM * NT_TN + e];
+    C[r + c * m] = v;
+  }
+}
+
+tq_status launch_gemm_native(const GemmJob &job_in, int64_t n_tiles, tq_dtype dt, cudaStream_t s,
+                             const NativeWork *w) {
+  GemmJob job = job_in;
+  if (w && w->chunks) {
+    job.tile_start = w->work_start;
+    job.chunks = w->chunks;
+    job.split_off = w->split_off;
+    job.kfused = w->kfused;
+    job.scratch = w->scratch;
+    n_tiles = w->n_work;
+  }
   const int64_t max_grid = 0x7fffffff;
   for (int64_t base = 0; base < n_tiles; base += max_grid) {
     const unsigned g = (unsigned)std::min<int64_t>(max_grid, n_tiles - base);
@@ -134,6 +208,16 @@ tq_status launch_gemm_native(const GemmJob &job, int64_t n_tiles, tq_dtype dt, c
     else
       count_launch(), gemm_native_kernel<float><<<g, NT_THREADS, 0, s>>>(job, base);
     TQ_CUDA(cudaGetLastError());
+  }
+  if (w && w->chunks) {
+    for (int64_t base = 0; base < w->n_split; base += max_grid) {
+      const unsigned g = (unsigned)std::min<int64_t>(max_grid, w->n_split - base);
+      if (dt == TQ_F64)
+        count_launch(), split_reduce_kernel<double><<<g, NT_THREADS, 0, s>>>(job, w->split_start, base);
+      else
+        count_launch(), split_reduce_kernel<float><<<g, NT_THREADS, 0, s>>>(job, w->split_start, base);
+      TQ_CUDA(cudaGetLastError());
+    }
   }
   return TQ_OK;
 }

@@ -28,7 +28,8 @@
 // pass (one ilogb per row) only.
 //
 // Layout of the sliced operands in global memory (built by oz_slice_kernel):
-// for every operand block, row tiles of RT rows (128 for A, 96 for B); in a
+// for every operand block, row tiles of RT rows (128 for A, the tile width 32,
+// 64 or 96 for B); in a
 // row tile, k-steps of 16 columns; in a k-step, s slices of G = ceil(rows/8)
 // row groups; in a row group two 8x8 bf16 core matrices (k 0-7, 8-15) of 128
 // contiguous bytes.  That is exactly the shared-memory image tcgen05 reads
@@ -44,7 +45,7 @@ namespace tq {
 
 constexpr int OZ_THREADS = 320;  // warp 0: loads, warp 1: MMA, warps 2-9: epilogue
 constexpr uint32_t OZ_TMEM_COLS = 512;
-// TMEM: OZ_NACC + 1 slots of OZ_N columns (480 of 512)
+// TMEM: OZ_NACC + 1 slots of tile-width columns (at most 480 of 512)
 constexpr int OZ_NACC = 4;
 constexpr int OZ_SMEM_BYTES = 200 * 1024;
 
@@ -318,6 +319,7 @@ struct OzTile {
 };
 
 // Global tile t of the launch -> its job and (output block, row tile, column tile).
+template <int N>
 __device__ __forceinline__ void oz_decode(const OzLaunch &L, int64_t t, OzTile &T) {
   const int64_t j = oz_find(L.job_tile_start, L.n_jobs, t);
   const OzJob &J = L.jobs[j];
@@ -336,13 +338,14 @@ __device__ __forceinline__ void oz_decode(const OzLaunch &L, int64_t t, OzTile &
   T.mt = local % tiles_m;
   T.nt = local / tiles_m;
   const int64_t ra = min((int64_t)OZ_M, T.m - T.mt * OZ_M);
-  const int64_t rb = min((int64_t)OZ_N, T.n - T.nt * OZ_N);
+  const int64_t rb = min((int64_t)N, T.n - T.nt * N);
   T.ga = (int32_t)((ra + 7) / 8);
   T.gb = (int32_t)((rb + 7) / 8);
   T.nmma = (int32_t)(16 * ((rb + 15) / 16));
   T.ksum = J.ksum[T.o];
 }
 
+template <int N>
 __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full_bar[OZ_MAX_STAGES], empty_bar[OZ_MAX_STAGES];
@@ -353,7 +356,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
   const int NS = L.nstages;
   // stages are sized for the largest slice count of the batch
   const uint32_t a_bytes_max = (uint32_t)L.s_max * (OZ_M / 8) * 256;
-  const uint32_t stage_bytes = (uint32_t)L.s_max * ((OZ_M + OZ_N) / 8) * 256;
+  const uint32_t stage_bytes = (uint32_t)L.s_max * ((OZ_M + N) / 8) * 256;
 
   if (threadIdx.x == 0) {
     for (int q = 0; q < NS; q++) {
@@ -380,7 +383,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       uint32_t it = 0;
       for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
         OzTile T;
-        oz_decode(L, t, T);
+        oz_decode<N>(L, t, T);
         // job fields in registers: the asm memory clobbers below would reload them
         const OzJob &J = *T.J;
         const int s = J.s;
@@ -393,7 +396,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
           const int64_t i = pa[p], j = pb[p];
           const int64_t nk = nk_pair[p];
           const uint8_t *ga = sliceA + 256 * unitA[i] + nk * s * 256 * (OZ_M / 8) * T.mt;
-          const uint8_t *gb = sliceB + 256 * unitB[j] + nk * s * 256 * (OZ_N / 8) * T.nt;
+          const uint8_t *gb = sliceB + 256 * unitB[j] + nk * s * 256 * (N / 8) * T.nt;
           for (int64_t q = 0; q < nk; q++, it++) {
             const uint32_t st = it % NS, use = it / NS;
             if (use > 0 && !mbar_wait(&empty_bar[st], (use - 1) & 1)) {
@@ -426,7 +429,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       for (int a = 0; a < OZ_NACC; a++) map |= (uint32_t)a << (3 * a);
       for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
         OzTile T;
-        oz_decode(L, t, T);
+        oz_decode<N>(L, t, T);
         const OzJob &J = *T.J;
         const int s = J.s;
         const int n_acc = s < OZ_NACC ? s : OZ_NACC;
@@ -467,7 +470,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
             tc_fence_after();
             uint32_t col[OZ_NACC];
 #pragma unroll
-            for (int a = 0; a < OZ_NACC; a++) col[a] = tmem + ((map >> (3 * a)) & 7) * OZ_N;
+            for (int a = 0; a < OZ_NACC; a++) col[a] = tmem + ((map >> (3 * a)) & 7) * N;
             const uint32_t sa = smem_u32(smem + st * stage_bytes);
             oz_issue_s(s, col, smem_desc(sa, 128, 256), smem_desc(sa + a_bytes_max, 128, 256),
                        (uint32_t)T.ga * 16, (uint32_t)T.gb * 16, idesc, fresh);
@@ -505,7 +508,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
     const int half = (warp - 2) >> 2;
     const int row = 32 * q4 + lane;
     const uint32_t lane_addr = tmem + ((uint32_t)(32 * q4) << 16);
-    const int cbase = half * (OZ_N / 2);
+    const int cbase = half * (N / 2);
     // the MMA warp's slot map, replayed: accumulator a in bits [3a, 3a+3),
     // bit p of `par` = parity of the drains of slot p so far
     uint32_t map = 0, par = 0;
@@ -514,7 +517,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
     for (int a = 0; a < OZ_NACC; a++) map |= (uint32_t)a << (3 * a);
     for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
       OzTile T;
-      oz_decode(L, t, T);
+      oz_decode<N>(L, t, T);
       const OzJob &J = *T.J;
       const int n_acc = J.s < OZ_NACC ? J.s : OZ_NACC;
       const int64_t grow = T.mt * OZ_M + row;
@@ -526,9 +529,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       int kb = 0;
       while (kb < 40 && (int64_t(1) << kb) < 16 * T.ksum) kb++;
       const int u = 48 - kb < 32 ? 48 - kb : 32;
-      long long S[OZ_N / 2];
+      long long S[N / 2];
 #pragma unroll
-      for (int y = 0; y < OZ_N / 2; y++) S[y] = 0;
+      for (int y = 0; y < N / 2; y++) S[y] = 0;
       OzSchedule sch;
       sch.start(T.ksum, n_acc);
       bool done = false;
@@ -552,17 +555,17 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
           const float scale = a < OZ_NACC - 1 ? __int_as_float((127 + 8 * a) << 23)
                                               : __int_as_float((127 + u) << 23);
           const int shift = a < OZ_NACC - 1 ? u - 8 * a : 0;
-          uint32_t v[OZ_N / 16][8];
+          uint32_t v[N / 16][8];
 #pragma unroll
-          for (int x = 0; x < OZ_N / 16; x++)
-            tmem_ld8(lane_addr + p * OZ_N + cbase + 8 * x, v[x]);
+          for (int x = 0; x < N / 16; x++)
+            tmem_ld8(lane_addr + p * N + cbase + 8 * x, v[x]);
           tmem_ld_wait();
           tc_fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(&slot_empty[p]);
           par ^= 1u << p;
 #pragma unroll
-          for (int x = 0; x < OZ_N / 16; x++)
+          for (int x = 0; x < N / 16; x++)
 #pragma unroll
             for (int y = 0; y < 8; y++)
               S[8 * x + y] += (long long)oz_to_int(__uint_as_float(v[x][y]), scale) << shift;
@@ -580,8 +583,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       const int32_t *expB = J.expB;
       if (row_ok) {
 #pragma unroll
-        for (int y = 0; y < OZ_N / 2; y++) {
-          const int64_t gcol = T.nt * OZ_N + cbase + y;
+        for (int y = 0; y < N / 2; y++) {
+          const int64_t gcol = T.nt * N + cbase + y;
           if (gcol < T.n) {
             const int fc = expB[rowB + gcol];
             C[grow + gcol * T.m] = oz_i64_ldexp(S[y], er + fc - 16 - u);
@@ -599,8 +602,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
 }
 
 // ---------------------------------------------------------------- host side
-int oz_stages(int s) {
-  const int stage = s * ((OZ_M + OZ_N) / 8) * 256;
+int oz_stages(int s, int tile_n) {
+  const int stage = s * ((OZ_M + tile_n) / 8) * 256;
   int n = OZ_SMEM_BYTES / stage;
   return n > OZ_MAX_STAGES ? OZ_MAX_STAGES : n;
 }
@@ -614,10 +617,15 @@ tq_status oz_batch_build(const std::vector<OzJob> &jobs, const std::vector<OzSid
   std::vector<int64_t> pre((nj + 1) + 3 * (ns + 1), 0);
   int64_t *jt = pre.data(), *sr = jt + nj + 1, *stl = sr + ns + 1, *se = stl + ns + 1;
   int s_max = 1;
+  const int tile_n = nj ? jobs[0].tile_n : OZ_N;
   for (int64_t j = 0; j < nj; j++) {
     jt[j + 1] = jt[j] + jobs[j].n_tiles;
     s_max = jobs[j].s > s_max ? jobs[j].s : s_max;
+    if (jobs[j].tile_n != tile_n)
+      return fail(TQ_ERR_INVALID, "the jobs of one tensor-core launch must share the tile width");
   }
+  if (tile_n != 32 && tile_n != 64 && tile_n != 96)
+    return fail(TQ_ERR_INVALID, "tile width must be 32, 64 or 96");
   for (int64_t k = 0; k < ns; k++) {
     sr[k + 1] = sr[k] + sides[k].n_rows;
     stl[k + 1] = stl[k] + sides[k].n_tiles;
@@ -648,7 +656,8 @@ tq_status oz_batch_build(const std::vector<OzJob> &jobs, const std::vector<OzSid
   L.n_slice_tiles = stl[ns];
   L.n_exps = se[ns];
   L.s_max = s_max;
-  L.nstages = oz_stages(s_max);
+  L.tile_n = tile_n;
+  L.nstages = oz_stages(s_max, tile_n);
   L.err = out.err.p;
   return TQ_OK;
 }
@@ -674,7 +683,11 @@ static tq_status oz_setup(int *sms) {
   if (!g_sms[dev]) {
     int n = 0;
     TQ_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
-    TQ_CUDA(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    TQ_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 OZ_SMEM_BYTES));
+    TQ_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 OZ_SMEM_BYTES));
+    TQ_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<96>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  OZ_SMEM_BYTES));
     g_sms[dev] = n;
   }
@@ -686,7 +699,12 @@ tq_status oz_batch_gemm(const OzBatchDev &b, cudaStream_t st) {
   const OzLaunch &L = b.L;
   if (L.n_tiles == 0) return TQ_OK;
   const int64_t grid = L.n_tiles < b.sms ? L.n_tiles : b.sms;
-  count_launch(), oz_gemm_kernel<<<(unsigned)grid, OZ_THREADS, OZ_SMEM_BYTES, st>>>(L);
+  count_launch();
+  switch (L.tile_n) {
+    case 32: oz_gemm_kernel<32><<<(unsigned)grid, OZ_THREADS, OZ_SMEM_BYTES, st>>>(L); break;
+    case 64: oz_gemm_kernel<64><<<(unsigned)grid, OZ_THREADS, OZ_SMEM_BYTES, st>>>(L); break;
+    default: oz_gemm_kernel<96><<<(unsigned)grid, OZ_THREADS, OZ_SMEM_BYTES, st>>>(L); break;
+  }
   TQ_CUDA(cudaGetLastError());
   return TQ_OK;
 }

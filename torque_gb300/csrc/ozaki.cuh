@@ -7,7 +7,9 @@
 namespace tq {
 
 constexpr int OZ_M = 128;        // output rows per tile (A side, TMEM lanes)
-constexpr int OZ_N = 96;         // output columns per tile (B side)
+constexpr int OZ_N = 96;         // widest tile: output columns per tile (B side)
+// tile widths the GEMM is instantiated for (the schedule's choice per launch)
+constexpr int OZ_TILE_NS[3] = {32, 64, 96};
 constexpr int OZ_CHUNK = 21;     // most k-steps of 16 an accumulator holds (K = 336)
 constexpr int OZ_MAXS = 7;       // most slices supported
 constexpr int OZ_MAX_STAGES = 8;
@@ -44,6 +46,7 @@ struct OzJob {
   const int64_t *rowA, *rowB;
   const int32_t *expA, *expB;
   int32_t s;
+  int32_t tile_n;             // output columns per tile (every job of a launch alike)
 };
 
 // Kernel parameter of a batched launch (arrays in device memory).
@@ -58,7 +61,7 @@ struct OzLaunch {
   const int64_t *side_exp_start;   // [n_sides+1]
   int32_t n_sides;
   int64_t n_rows, n_slice_tiles, n_exps;
-  int32_t s_max, nstages;
+  int32_t s_max, nstages, tile_n;
   int32_t *err;
 };
 
@@ -72,7 +75,7 @@ struct OzBatchDev {
   int sms = 0;  // multiprocessors of the device: the persistent grid
 };
 
-int oz_stages(int s);
+int oz_stages(int s, int tile_n);
 tq_status oz_batch_build(const std::vector<OzJob> &jobs, const std::vector<OzSide> &sides,
                          cudaStream_t s, OzBatchDev &out);
 // Row exponents and slices of every side of the batch.

@@ -3,8 +3,19 @@
 #pragma once
 #include <memory>
 
+#include "gemm.cuh"
 #include "ozaki.cuh"
 #include "tq_internal.h"
+
+namespace tq {
+// Device arrays behind a NativeWork (split-K work list of the native kernel).
+struct NativeWorkDev {
+  DevArray<int32_t> chunks;
+  DevArray<int64_t> kfused, work_start, split_start, split_off;
+  DevArray<uint8_t> scratch;
+  NativeWork w;
+};
+}  // namespace tq
 
 struct tq_plan {
   const tq_bs *A = nullptr, *B = nullptr;
@@ -19,6 +30,7 @@ struct tq_plan {
   tq::DevArray<int64_t> tile_start;       // [n_out+1]
   tq::DevArray<int64_t> chunk_start;      // rank-0 results
   tq::DevArray<double> partials;          // rank-0 results (float partials use the low half)
+  tq::NativeWorkDev nat;                  // native kernel work list (all outputs)
   // tensor-core (sliced) forms
   int32_t slices = 0;
   bool tc = false;
@@ -31,6 +43,14 @@ struct tq_plan {
   tq::DevArray<int32_t> expA, expB, nk_pair;
   tq::DevArray<uint8_t> sliceA, sliceB;
   int64_t rowsA = 0, rowsB = 0, tilesA = 0, tilesB = 0, nexpA = 0, nexpB = 0, tc_tiles = 0;
+  int32_t tile_n = 0;
+  int64_t KA = 0, KB = 0;  // free-box key ranges (tensor-core plans, reduced layout)
+  bool keys = false;       // keyA/keyB were made
+  bool sched_ok = true;    // false after a failed reschedule: execute refuses
+  // block grouping: native 64x64 tiles of the outputs sent to plain FP64
+  tq::DevArray<int64_t> hyb_tile_start;
+  int64_t hyb_tiles = 0;
+  tq::NativeWorkDev hyb;
   tq::OzJob tc_job{};              // this contraction as one job
   tq::OzSide tc_side[2]{};         // its A and B operand sides
   tq::OzBatchDev tcb;              // the same as a batch of one, on the device
@@ -44,6 +64,10 @@ struct tq_plan {
 };
 
 namespace tq {
+tq_status run_hybrid_native(tq_plan *P, cudaStream_t s);
+tq_status plan_run(tq_plan *P, cudaStream_t s);
+tq_status plan_check(tq_plan *P, cudaStream_t s);
+tq_status plan_reschedule(tq_plan *P, const tq_contract_opts &o, cudaStream_t s);
 tq_status validate_legs(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,
                         const int64_t *b_legs, LegSpec &L);
 }

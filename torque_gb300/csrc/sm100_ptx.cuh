@@ -1,8 +1,8 @@
 // Thin inline-PTX wrappers for the Blackwell (sm_100 family, sm_103a here)
 // features the tensor-core kernels use: mbarriers with bounded waits, bulk
 // (TMA engine) copies global -> shared, and tcgen05 (TMEM allocation, MMA,
-// commit, TMEM loads/stores).  Every wait gives up after a bounded number of
-// polls and reports it, so no kernel can spin forever.
+// commit, TMEM loads/stores).  Every wait gives up after a bounded wall time
+// (the global nanosecond timer) and reports it, so no kernel can spin forever.
 #pragma once
 #include <stdint.h>
 
@@ -49,14 +49,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return done != 0;
 }
 
-// Bounded wait: true when the phase completed, false after ~max_polls polls.
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait: true when the phase completed, false once the wait has lasted
+// about max_ns nanoseconds of wall time (a healthy pipeline waits microseconds).
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
-                                          uint32_t max_polls = (1u << 26)) {
-  for (uint32_t i = 0; i < max_polls; i++) {
+                                          uint64_t max_ns = 2000000000ull) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (uint32_t i = 1;; i++) {
     if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 255) == 0 && global_ns() - t0 > max_ns) return false;
     if (i > 64) __nanosleep(64);
   }
-  return false;
 }
 
 // Bulk copy global -> shared through the TMA engine, completing on `bar`.

@@ -70,14 +70,18 @@ class BlockList:
 def charge_blocks(legs: List[Leg], total: int = 0, modulus: Optional[int] = None) -> BlockList:
     """All sector tuples with sum(direction * charge) == total (mod `modulus`
     for Z_n symmetries), in column-major order of the sector indices."""
-    shape = [len(l.charges) for l in legs]
-    grids = np.meshgrid(*[np.arange(n) for n in shape], indexing="ij")
-    sidx = np.stack([g.ravel(order="F") for g in grids], axis=1).astype(np.int64)
-    q = np.zeros(sidx.shape[0], np.int64)
-    for l, leg in enumerate(legs):
-        q += leg.direction * np.asarray(leg.charges, np.int64)[sidx[:, l]]
-    keep = ((q - total) % modulus == 0) if modulus else (q == total)
-    sidx = sidx[keep]
+    if modulus or not legs:
+        shape = [len(l.charges) for l in legs]
+        grids = np.meshgrid(*[np.arange(n) for n in shape], indexing="ij")
+        sidx = np.stack([g.ravel(order="F") for g in grids], axis=1).astype(np.int64)
+        sidx = sidx.reshape(-1, len(legs))
+        q = np.zeros(sidx.shape[0], np.int64)
+        for l, leg in enumerate(legs):
+            q += leg.direction * np.asarray(leg.charges, np.int64)[sidx[:, l]]
+        keep = ((q - total) % modulus == 0) if modulus else (q == total)
+        sidx = sidx[keep]
+    else:
+        sidx = _u1_tuples(legs, total)
     begin = np.zeros_like(sidx)
     end = np.zeros_like(sidx)
     for l, leg in enumerate(legs):
@@ -87,6 +91,33 @@ def charge_blocks(legs: List[Leg], total: int = 0, modulus: Optional[int] = None
         end[:, l] = off[sidx[:, l]] + sz[sidx[:, l]] - 1
     dim = np.asarray([leg.dim for leg in legs], np.int64)
     return BlockList(dim, begin, end, sidx)
+
+
+def _u1_tuples(legs: List[Leg], total: int) -> np.ndarray:
+    """Sector tuples of U(1) legs with sum(direction * charge) == total, built
+    leg by leg and pruned by the charge range the remaining legs can still
+    add; returned in column-major order (leg 0 fastest)."""
+    qs = [leg.direction * np.asarray(leg.charges, np.int64) for leg in legs]
+    lo = np.zeros(len(legs) + 1, np.int64)
+    hi = np.zeros(len(legs) + 1, np.int64)
+    for l in range(len(legs) - 1, -1, -1):
+        lo[l] = lo[l + 1] + qs[l].min()
+        hi[l] = hi[l + 1] + qs[l].max()
+    part = np.zeros((1, 0), np.int64)
+    charge = np.zeros(1, np.int64)
+    for l in range(len(legs)):
+        n = len(qs[l])
+        rep = np.repeat(np.arange(part.shape[0]), n)
+        idx = np.tile(np.arange(n, dtype=np.int64), part.shape[0])
+        c = charge[rep] + qs[l][idx]
+        need = total - c
+        ok = (need >= lo[l + 1]) & (need <= hi[l + 1])
+        part = np.concatenate([part[rep[ok]], idx[ok, None]], axis=1)
+        charge = c[ok]
+    if part.shape[0] == 0:
+        return part
+    order = np.lexsort(part.T)  # last key primary: leg 0 varies fastest
+    return part[order]
 
 
 def gaussian_sizes(charges: Sequence[int], peak: float, width2: float) -> List[int]:

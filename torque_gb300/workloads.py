@@ -150,3 +150,111 @@ def peps_sweep(n: int = 256, seed: int = 3, data: bool = True):
             t = e1 = e2 = np.zeros(0)
         out.append(SiteUpdate(D, chi, T, E1, E2, t, e1, e2))
     return out
+
+
+# ---------------------------------------------------------------- random contractions
+@dataclass
+class RandomContraction:
+    """One random U(1) block-sparse contraction: A's legs a_legs[k] contract
+    with B's legs b_legs[k] (pairs = [[a_legs[k], b_legs[k]]])."""
+    index: int
+    A: BlockList
+    B: BlockList
+    pairs: np.ndarray
+    a_legs: list
+    b_legs: list
+
+
+def _profile_sizes(dim: int, n: int, gaussian: bool):
+    """n sector sizes summing to dim (each >= 1): Gaussian weights
+    exp(-q^2 / (2 (n/4)^2)) over q = -(n//2).., or uniform; largest remainder."""
+    q = np.arange(n) - n // 2
+    w = np.exp(-q.astype(float) ** 2 / (2.0 * max(1.0, n / 4.0) ** 2)) if gaussian else np.ones(n)
+    raw = w / w.sum() * dim
+    s = np.maximum(1, np.floor(raw)).astype(int)
+    while s.sum() < dim:
+        s[np.argmax(raw - s)] += 1
+    while s.sum() > dim:
+        k = np.argmax(np.where(s > 1, s - raw, -np.inf))
+        s[k] -= 1
+    return q.tolist(), s.tolist()
+
+
+def _n_charge_tuples(legs) -> int:
+    """Blocks charge_blocks(legs) would produce, by convolving charge counts."""
+    dist = {0: 1}
+    for leg in legs:
+        nd = {}
+        for q0, c0 in dist.items():
+            for q in leg.charges:
+                k = q0 + leg.direction * q
+                nd[k] = nd.get(k, 0) + c0
+        dist = nd
+    return dist.get(0, 0)
+
+
+def random_contractions(n: int = 2000, seed: int = 4, max_elem: int = 1 << 22,
+                        max_blocks: int = 50000, max_flops: float = 2e10):
+    """n random U(1) contractions, seeded: ranks 3-6, leg dims log-uniform in
+    16..1024, 2-41 sectors per leg (consecutive charges around 0) with a
+    Gaussian or uniform size profile, 1-3 contracted legs (A outgoing, B
+    incoming), free-leg directions random.  Caps, so that one GPU runs every
+    candidate schedule of all n in minutes: each tensor at most max_elem
+    elements and max_blocks blocks, the contraction at most max_flops useful
+    flops (legs are halved, largest first, and sector counts lowered until the
+    caps hold).  Entries are not drawn here: the caller fills N(0,1) data."""
+    rng = np.random.default_rng(seed)
+    out = []
+    i = 0
+    while len(out) < n:
+        ra, rb = int(rng.integers(3, 7)), int(rng.integers(3, 7))
+        nc = int(rng.integers(1, min(3, ra - 1, rb - 1) + 1))
+        nlegs = ra + rb - nc
+        dims = np.exp(rng.uniform(np.log(16), np.log(1024), nlegs)).astype(int)
+        nsec = rng.integers(2, 42, nlegs)
+        gauss = rng.random(nlegs) < 0.5
+        dirs = rng.choice([-1, 1], nlegs)
+        # legs 0..nc-1 are the contracted ones; A = [free A..., contracted], B = [contracted, free B...]
+        perm_a = rng.permutation(ra)
+        perm_b = rng.permutation(rb)
+        for _ in range(64):
+            nsec = np.minimum(nsec, dims)
+
+            def leg(j, d):
+                q, s = _profile_sizes(int(dims[j]), int(nsec[j]), bool(gauss[j]))
+                return Leg(q, s, d)
+            con = [leg(j, -1) for j in range(nc)]
+            fa = [leg(nc + j, int(dirs[nc + j])) for j in range(ra - nc)]
+            fb = [leg(ra + j, int(dirs[ra + j])) for j in range(rb - nc)]
+            a_list = fa + con
+            b_list = [c.flipped() for c in con] + fb
+            a_order = [a_list[p] for p in perm_a]
+            b_order = [b_list[p] for p in perm_b]
+            nba, nbb = _n_charge_tuples(a_order), _n_charge_tuples(b_order)
+            fill = lambda legs, nb: nb * np.prod([l.dim / len(l.sizes) for l in legs])
+            ea, eb = fill(a_order, nba), fill(b_order, nbb)
+            if nba <= max_blocks and nbb <= max_blocks and ea <= 2 * max_elem and eb <= 2 * max_elem:
+                A = charge_blocks(a_order)
+                B = charge_blocks(b_order)
+                a_pos = {p: k for k, p in enumerate(perm_a)}
+                b_pos = {p: k for k, p in enumerate(perm_b)}
+                a_legs = [a_pos[ra - nc + c] for c in range(nc)]
+                b_legs = [b_pos[c] for c in range(nc)]
+                pairs = np.array([[a, b] for a, b in zip(a_legs, b_legs)], np.int64)
+                if (A.n_elem <= max_elem and B.n_elem <= max_elem and A.n_blocks and B.n_blocks
+                        and useful_flops(A, B, pairs) <= max_flops):
+                    break
+            # shrink: halve the largest leg, or lower the most split leg's sector count
+            j = int(np.argmax(dims))
+            if dims[j] > 16:
+                dims[j] = max(16, dims[j] // 2)
+            else:
+                k = int(np.argmax(nsec))
+                nsec[k] = max(2, nsec[k] // 2)
+        else:
+            i += 1
+            continue
+        if useful_flops(A, B, pairs) > 0:
+            out.append(RandomContraction(i, A, B, pairs, a_legs, b_legs))
+        i += 1
+    return out
