@@ -226,16 +226,24 @@ __device__ __forceinline__ double oz_i64_ldexp(long long T, int e) {
 
 // ---------------------------------------------------------------- the GEMM
 // Accumulators by g = t+u: D0, D1, D2 (exact) and D3 (g >= 3, rounded).  They
-// live in OZ_NSLOT TMEM slots of OZ_N columns, one more slot than accumulators:
-// accumulator a is retired after every OZ_CHUNK k-steps on its own staggered
-// schedule (first after OZ_CHUNK - OZ_STAG*a), moved into the spare slot, and
-// the retired slot is drained by the epilogue while the MMAs go on.  Each slot
-// has its own full/empty barrier pair, so no parity wait can fall two phases
-// behind: a slot is never retired twice without a drain in between.
-constexpr int OZ_NSLOT = OZ_NACC + 1;
+// live in TMEM slots of tile-width columns, more slots than accumulators (five
+// for width 96, eight for 32 and 64): accumulator a is retired after every
+// OZ_CHUNK k-steps on its own staggered schedule (first after
+// OZ_CHUNK - OZ_STAG*a), and at the end of its tile; it then restarts in the
+// free slot retired longest ago, and the retired slot is drained by the
+// epilogue while the MMAs go on.  With eight slots a whole tile's accumulators
+// move to fresh slots at its end, so the next tile's MMAs start before the
+// epilogue has drained the last one.  Each slot has its own full/empty barrier
+// pair, so no parity wait can fall two phases behind: a slot is never retired
+// twice without a drain in between.
+constexpr int OZ_MAXSLOT = 2 * OZ_NACC;
 constexpr int OZ_STAG = 5;
 constexpr int OZ_FINAL = 100;
-static_assert(OZ_NSLOT * OZ_N <= (int)OZ_TMEM_COLS, "slots exceed TMEM");
+template <int N>
+struct OzSlots {
+  static constexpr int n = (int)OZ_TMEM_COLS / N >= 2 * OZ_NACC ? 2 * OZ_NACC : OZ_NACC + 1;
+  static_assert(n * N <= (int)OZ_TMEM_COLS, "slots exceed TMEM");
+};
 static_assert(OZ_STAG * (OZ_NACC - 1) < OZ_CHUNK, "stagger must fit one chunk");
 
 // All slice products of one k-step, fully unrolled: product (t, u) goes to
@@ -349,7 +357,8 @@ template <int N>
 __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full_bar[OZ_MAX_STAGES], empty_bar[OZ_MAX_STAGES];
-  __shared__ __align__(8) uint64_t slot_full[OZ_NSLOT], slot_empty[OZ_NSLOT], done_bar;
+  __shared__ __align__(8) uint64_t slot_full[OZ_MAXSLOT], slot_empty[OZ_MAXSLOT], done_bar;
+  constexpr int NSLOT = OzSlots<N>::n;
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_flag;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -363,7 +372,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       mbar_init(&full_bar[q], 1);
       mbar_init(&empty_bar[q], 1);
     }
-    for (int q = 0; q < OZ_NSLOT; q++) {
+    for (int q = 0; q < NSLOT; q++) {
       mbar_init(&slot_full[q], 1);
       mbar_init(&slot_empty[q], 8);
     }
@@ -424,9 +433,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       // slot of accumulator a in bits [3a, 3a+3); per slot p: bit p of `par` is
       // the parity of its completed uses, bit p of `used` whether it had one
       uint32_t map = 0, par = 0, used = 0;
-      int spare = OZ_NACC;
+      // free slots, 3 bits each, oldest retirement first (always NSLOT - OZ_NACC)
+      uint32_t fifo = 0;
+      constexpr int NFREE = NSLOT - OZ_NACC;
 #pragma unroll
       for (int a = 0; a < OZ_NACC; a++) map |= (uint32_t)a << (3 * a);
+#pragma unroll
+      for (int q = 0; q < NFREE; q++) fifo |= (uint32_t)(OZ_NACC + q) << (3 * q);
       for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
         OzTile T;
         oz_decode<N>(L, t, T);
@@ -484,11 +497,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
                 mma_commit(&slot_full[p]);
                 par ^= 1u << p;
                 used |= 1u << p;
-                if (ev_kind != OZ_FINAL) {  // restart a in the spare slot
-                  map = (map & ~(7u << (3 * a))) | ((uint32_t)spare << (3 * a));
-                  spare = (int)p;
-                  fresh |= 1u << a;
-                }
+                // restart a in the oldest free slot; p joins the free list
+                const uint32_t q = fifo & 7;
+                fifo = (fifo >> 3) | (p << (3 * (NFREE - 1)));
+                map = (map & ~(7u << (3 * a))) | (q << (3 * a));
+                fresh |= 1u << a;
               }
               if (ev_kind != OZ_FINAL) {
                 sch.advance(ev_kind);
@@ -511,10 +524,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
     const int cbase = half * (N / 2);
     // the MMA warp's slot map, replayed: accumulator a in bits [3a, 3a+3),
     // bit p of `par` = parity of the drains of slot p so far
-    uint32_t map = 0, par = 0;
-    int spare = OZ_NACC;
+    uint32_t map = 0, par = 0, fifo = 0;
+    constexpr int NFREE = NSLOT - OZ_NACC;
 #pragma unroll
     for (int a = 0; a < OZ_NACC; a++) map |= (uint32_t)a << (3 * a);
+#pragma unroll
+    for (int q = 0; q < NFREE; q++) fifo |= (uint32_t)(OZ_NACC + q) << (3 * q);
     for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
       OzTile T;
       oz_decode<N>(L, t, T);
@@ -569,11 +584,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
 #pragma unroll
             for (int y = 0; y < 8; y++)
               S[8 * x + y] += (long long)oz_to_int(__uint_as_float(v[x][y]), scale) << shift;
-          if (!done) {
-            map = (map & ~(7u << (3 * a))) | ((uint32_t)spare << (3 * a));
-            spare = (int)p;
-            sch.advance(a);
-          }
+          const uint32_t q = fifo & 7;
+          fifo = (fifo >> 3) | (p << (3 * (NFREE - 1)));
+          map = (map & ~(7u << (3 * a))) | (q << (3 * a));
+          if (!done) sch.advance(a);
         }
       }
       if (abort_flag) break;

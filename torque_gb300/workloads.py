@@ -39,22 +39,29 @@ class Contraction:
 def useful_flops(A: BlockList, B: BlockList, pairs) -> float:
     """Sum over matched pairs of 2*m*n*k, for sector-aligned boxes (pairs match
     iff their contracted boxes are equal), grouped by contracted box."""
+    return pair_stats(A, B, pairs)[0]
+
+
+def pair_stats(A: BlockList, B: BlockList, pairs):
+    """(useful flops, matched pairs) of a sector-aligned contraction."""
     pairs = np.asarray(pairs).reshape(-1, 2)
     al, bl = pairs[:, 0], pairs[:, 1]
     fa = [l for l in range(A.begin.shape[1]) if l not in set(al.tolist())]
     fb = [l for l in range(B.begin.shape[1]) if l not in set(bl.tolist())]
     da, db = A.block_dims, B.block_dims
-    m = np.prod(da[:, fa], axis=1) if fa else np.ones(A.n_blocks, np.int64)
-    n = np.prod(db[:, fb], axis=1) if fb else np.ones(B.n_blocks, np.int64)
-    k = np.prod(da[:, al], axis=1) if len(al) else np.ones(A.n_blocks, np.int64)
-    from collections import defaultdict
-    msum = defaultdict(float)
-    for key, mm, kk in zip(map(tuple, np.concatenate([A.begin[:, al], A.end[:, al]], 1)), m, k):
-        msum[key] += float(mm) * float(kk)
-    total = 0.0
-    for key, nn in zip(map(tuple, np.concatenate([B.begin[:, bl], B.end[:, bl]], 1)), n):
-        total += 2.0 * msum.get(key, 0.0) * float(nn)
-    return total
+    m = np.prod(da[:, fa], axis=1).astype(float) if fa else np.ones(A.n_blocks)
+    n = np.prod(db[:, fb], axis=1).astype(float) if fb else np.ones(B.n_blocks)
+    k = np.prod(da[:, al], axis=1).astype(float) if len(al) else np.ones(A.n_blocks)
+    ka = np.concatenate([A.begin[:, al], A.end[:, al]], 1)
+    kb = np.concatenate([B.begin[:, bl], B.end[:, bl]], 1)
+    keys, inv = np.unique(np.concatenate([ka, kb], 0), axis=0, return_inverse=True)
+    inv = inv.reshape(-1)
+    ia, ib = inv[:A.n_blocks], inv[A.n_blocks:]
+    mk = np.bincount(ia, weights=m * k, minlength=len(keys))
+    ca = np.bincount(ia, minlength=len(keys)).astype(float)
+    nb = np.bincount(ib, weights=n, minlength=len(keys))
+    cb = np.bincount(ib, minlength=len(keys)).astype(float)
+    return float(2.0 * np.sum(mk * nb)), int(np.sum(ca * cb))
 
 
 def u1_rank4(charges, sizes, seed: int, name: str) -> Contraction:
@@ -194,15 +201,17 @@ def _n_charge_tuples(legs) -> int:
 
 
 def random_contractions(n: int = 2000, seed: int = 4, max_elem: int = 1 << 22,
-                        max_blocks: int = 50000, max_flops: float = 2e10):
+                        max_blocks: int = 50000, max_flops: float = 2e10,
+                        max_pairs: int = 1 << 18):
     """n random U(1) contractions, seeded: ranks 3-6, leg dims log-uniform in
     16..1024, 2-41 sectors per leg (consecutive charges around 0) with a
     Gaussian or uniform size profile, 1-3 contracted legs (A outgoing, B
     incoming), free-leg directions random.  Caps, so that one GPU runs every
     candidate schedule of all n in minutes: each tensor at most max_elem
     elements and max_blocks blocks, the contraction at most max_flops useful
-    flops (legs are halved, largest first, and sector counts lowered until the
-    caps hold).  Entries are not drawn here: the caller fills N(0,1) data."""
+    flops and max_pairs matched block pairs (legs are halved, largest first,
+    and sector counts lowered until the caps hold).  Entries are not drawn
+    here: the caller fills N(0,1) data."""
     rng = np.random.default_rng(seed)
     out = []
     i = 0
@@ -217,6 +226,7 @@ def random_contractions(n: int = 2000, seed: int = 4, max_elem: int = 1 << 22,
         # legs 0..nc-1 are the contracted ones; A = [free A..., contracted], B = [contracted, free B...]
         perm_a = rng.permutation(ra)
         perm_b = rng.permutation(rb)
+        A = B = pairs = None
         for _ in range(64):
             nsec = np.minimum(nsec, dims)
 
@@ -233,6 +243,7 @@ def random_contractions(n: int = 2000, seed: int = 4, max_elem: int = 1 << 22,
             nba, nbb = _n_charge_tuples(a_order), _n_charge_tuples(b_order)
             fill = lambda legs, nb: nb * np.prod([l.dim / len(l.sizes) for l in legs])
             ea, eb = fill(a_order, nba), fill(b_order, nbb)
+            A = B = None
             if nba <= max_blocks and nbb <= max_blocks and ea <= 2 * max_elem and eb <= 2 * max_elem:
                 A = charge_blocks(a_order)
                 B = charge_blocks(b_order)
@@ -241,20 +252,24 @@ def random_contractions(n: int = 2000, seed: int = 4, max_elem: int = 1 << 22,
                 a_legs = [a_pos[ra - nc + c] for c in range(nc)]
                 b_legs = [b_pos[c] for c in range(nc)]
                 pairs = np.array([[a, b] for a, b in zip(a_legs, b_legs)], np.int64)
-                if (A.n_elem <= max_elem and B.n_elem <= max_elem and A.n_blocks and B.n_blocks
-                        and useful_flops(A, B, pairs) <= max_flops):
-                    break
-            # shrink: halve the largest leg, or lower the most split leg's sector count
+                if A.n_elem <= max_elem and B.n_elem <= max_elem and A.n_blocks and B.n_blocks:
+                    fl, npairs = pair_stats(A, B, pairs)
+                    if fl <= max_flops and npairs <= max_pairs:
+                        break
+            # shrink: too many blocks or pairs -> fewer sectors on the most split
+            # leg; too large -> halve the largest leg
+            many = nba > max_blocks or nbb > max_blocks or (
+                A is not None and B is not None and pair_stats(A, B, pairs)[1] > max_pairs)
             j = int(np.argmax(dims))
-            if dims[j] > 16:
-                dims[j] = max(16, dims[j] // 2)
-            else:
+            if many or dims[j] <= 16:
                 k = int(np.argmax(nsec))
                 nsec[k] = max(2, nsec[k] // 2)
+            else:
+                dims[j] = max(16, dims[j] // 2)
         else:
             i += 1
             continue
-        if useful_flops(A, B, pairs) > 0:
+        if pair_stats(A, B, pairs)[0] > 0:
             out.append(RandomContraction(i, A, B, pairs, a_legs, b_legs))
         i += 1
     return out
