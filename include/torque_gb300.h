@@ -151,6 +151,18 @@ tq_status tq_bs_contract(const tq_bs *A, const tq_bs *B, int32_t n_legs,
 tq_status tq_bs_hard_transpose(const tq_bs *t, const int64_t *perm, tq_stream stream,
                                tq_bs **out);
 
+/* Leg fusion (no reference counterpart; a PEPS double layer needs it): legs
+ * `leg` and `leg`+1 become one leg of dimension dim_a * dim_b.  Leg a is cut
+ * into n_sec_a sectors at bounds_a[0..n_sec_a] (bounds_a[0] = 0, last = dim),
+ * leg b likewise; sector pair (a, b) occupies the fused range starting at
+ * pair_offset[a + n_sec_a * b], of length size_a * size_b (the ranges must
+ * tile the fused leg).  Every block must cover whole sectors on both legs with
+ * contiguous strides across them; its data are then already in the fused
+ * layout and are copied unchanged. */
+tq_status tq_bs_fuse_legs(const tq_bs *t, int32_t leg, int64_t n_sec_a, const int64_t *bounds_a,
+                          int64_t n_sec_b, const int64_t *bounds_b, const int64_t *pair_offset,
+                          tq_stream stream, tq_bs **out);
+
 /* slice (block_sparse.cuh:1124-1176): split every block into prod(divisor)
  * boxes without moving data, as the reference does. */
 tq_status tq_bs_slice(const tq_bs *t, const int64_t *divisor, tq_stream stream,
@@ -222,7 +234,10 @@ typedef struct {
  * warm-up, then `reps` timed runs), measures its error against the plain FP64
  * result of the same plan, and sets *best to the fastest candidate whose error
  * is at most target_rel_err (-1: none).  The plan is left with the winner's
- * schedule (its own if none).  Synchronises; float64 tensors only. */
+ * schedule (its own if none).  A negative target times the candidates only
+ * (no FP64 reference run; rel_err = -1; the fastest wins): for tuning the tile
+ * width and grouping of a slice count already known to meet the target.
+ * Synchronises; float64 tensors only. */
 tq_status tq_autotune(tq_plan *plan, double target_rel_err, tq_tune_entry *cands,
                       int32_t n_cands, int32_t reps, int32_t *best, tq_stream stream);
 

@@ -220,6 +220,23 @@ class BlockSparseTensor {
     return BlockSparseTensor(out);
   }
 
+  // Legs `leg` and `leg`+1 fused into one (an extension: the reference has no
+  // leg fusion).  bounds_a / bounds_b: sector boundaries of the two legs (first
+  // 0, last the leg's dimension); pair_offset(a, b): where sector pair (a, b)
+  // starts in the fused leg.  See tq_bs_fuse_legs.
+  BlockSparseTensor fuse_legs(arma::uword leg, const arma::uvec &bounds_a,
+                              const arma::uvec &bounds_b, const arma::umat &pair_offset) const {
+    if (leg + 1 >= rank) throw Error("legs to fuse out of range");
+    if (pair_offset.n_rows + 1 != bounds_a.n_elem || pair_offset.n_cols + 1 != bounds_b.n_elem)
+      throw Error("pair_offset must be (sectors of a) x (sectors of b)");
+    const auto ba = detail::flat(bounds_a), bb = detail::flat(bounds_b),
+               off = detail::flat(pair_offset);
+    tq_bs *out = nullptr;
+    detail::check(tq_bs_fuse_legs(h_, (int32_t)leg, (int64_t)ba.size() - 1, ba.data(),
+                                  (int64_t)bb.size() - 1, bb.data(), off.data(), nullptr, &out));
+    return BlockSparseTensor(out);
+  }
+
   // the underlying handle, for calls of the C ABI not wrapped here
   tq_bs *handle() const { return h_; }
 

@@ -54,6 +54,7 @@ SIGNATURES = {
     "tq_bs_contract": (ST, [P, P, I32, P64, P64, ctypes.POINTER(ContractOpts), P, PP]),
     "tq_bs_hard_transpose": (ST, [P, P64, P, PP]),
     "tq_bs_slice": (ST, [P, P64, P, PP]),
+    "tq_bs_fuse_legs": (ST, [P, I32, I64, P64, I64, P64, P64, P, PP]),
     "tq_nest_sum": (ST, [P, I64, P, P, P]),
     "tq_nest_sum_noalloc": (ST, [P, I64, P, P, P]),
     "tq_plan_create": (ST, [P, P, I32, P64, P64, ctypes.POINTER(ContractOpts), P, PP, PP]),

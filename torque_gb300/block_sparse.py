@@ -241,6 +241,26 @@ class BlockSparseTensor:
         check(load().tq_bs_hard_transpose(self._h, _p64(perm), _stream(stream), ctypes.byref(h)))
         return BlockSparseTensor(_handle=h)
 
+    def fuse_legs(self, leg: int, bounds_a, bounds_b, pair_offset, stream=None):
+        """Legs leg and leg+1 fused (tq_bs_fuse_legs): bounds_* are the sector
+        boundaries of the two legs, pair_offset[a, b] the start of sector pair
+        (a, b) in the fused leg."""
+        ba, bb = _i64(bounds_a), _i64(bounds_b)
+        off = _i64(np.asarray(pair_offset).reshape(ba.size - 1, bb.size - 1).ravel(order="F"))
+        h = ctypes.c_void_p()
+        check(load().tq_bs_fuse_legs(self._h, int(leg), ba.size - 1, _p64(ba), bb.size - 1,
+                                     _p64(bb), _p64(off), _stream(stream), ctypes.byref(h)))
+        return BlockSparseTensor(_handle=h)
+
+    def fuse_sectors(self, leg: int, leg_a, leg_b, modulus=None, stream=None):
+        """Charge-ordered fusion of legs leg, leg+1 carrying sectors leg_a,
+        leg_b (sectors.Leg); returns (tensor, fused Leg)."""
+        from .sectors import fuse_sector_order
+        fused, off = fuse_sector_order(leg_a, leg_b, modulus)
+        ba = np.concatenate([[0], np.cumsum(leg_a.sizes)])
+        bb = np.concatenate([[0], np.cumsum(leg_b.sizes)])
+        return self.fuse_legs(leg, ba, bb, off, stream), fused
+
     def slice(self, divisor, stream=None) -> "BlockSparseTensor":
         d = _i64(divisor)
         h = ctypes.c_void_p()

@@ -23,6 +23,8 @@ forward, backward and update is a library kernel).
 from __future__ import annotations
 
 import ctypes
+import json
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -32,6 +34,13 @@ from ._lib import check, load
 
 PENALTY = 4.0
 TARGETS = (1e-6, 1e-8, 1e-10, 1e-12)
+
+_DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+# the exhaustive tuner's measurements of the 2,000 random contractions of seed 4
+# (made on a GB300 by `python -m torque_gb300.costmodel --n 2000 --seed 4`)
+DATASET = os.path.join(_DATA, "tune_random_s4.npz")
+# the held-out contractions' structure (workloads.RandomContraction.spec)
+HELD_OUT = os.path.join(_DATA, "random_s4_heldout.json")
 
 
 def _cands():
@@ -225,6 +234,64 @@ def evaluate(records, choice_fn, target):
     return np.asarray(out)
 
 
+# ---------------------------------------------------------------- evaluation
+DEFAULT_SLICES = {1e-6: 3, 1e-8: 4, 1e-10: 5, 1e-12: 6}
+
+
+def default_choice(eps):
+    """The schedule the library takes without the model: the slice count the
+    target asks for (3 / 4 / 5 / 6 slices for 1e-6 / 1e-8 / 1e-10 / 1e-12),
+    tile width 96, no grouping."""
+    s = DEFAULT_SLICES.get(eps, 5)
+    for i, c in enumerate(CANDIDATES):
+        if c.get("slices") == s and c.get("tile_n") == 96 and c.get("native_fill") == 0:
+            return i
+    raise KeyError(s)
+
+
+def split(records, n_test=200):
+    """Training and held-out records: the last n_test by draw order are held out."""
+    return records[:-n_test], records[-n_test:]
+
+
+def train(records, seed=0, steps=3000, lr=2e-3, width=64, log_every=0):
+    X, T = training_arrays(records)
+    net = MLP(width=width, seed=seed)
+    curve = net.fit(X, T, steps=steps, lr=lr, log_every=log_every)
+    return net, curve
+
+
+def model_choices(net, records, eps):
+    X = np.array([r.features for r in records], np.float32)
+    X[:, 0] = -np.log10(eps) / 16.0
+    return net.propose(X)
+
+
+def regret_report(records, choices, eps):
+    """Per-target comparison of a chooser with the exhaustive tuner over
+    records: mean / median / p90 of ms_chosen / ms_best - 1 (feasible picks),
+    share of picks whose error misses eps, and total times."""
+    rg, miss, t_pick, t_best, fl = [], 0, 0.0, 0.0, 0.0
+    for r, c in zip(records, choices):
+        b = best_feasible(r.ms, r.err, r.status, eps)
+        if b < 0:
+            continue
+        ok = r.status[c] == 0 and r.err[c] <= eps
+        if not ok:
+            miss += 1
+            c = b  # the exhaustive tuner is the fallback
+        rg.append(r.ms[c] / r.ms[b] - 1.0)
+        t_pick += r.ms[c]
+        t_best += r.ms[b]
+        fl += r.flops
+    rg = np.asarray(rg)
+    return dict(target=eps, n=len(rg), mean_regret=float(rg.mean()),
+                median_regret=float(np.median(rg)), p90_regret=float(np.percentile(rg, 90)),
+                miss_rate=miss / max(len(rg), 1), ms_total=t_pick, ms_best_total=t_best,
+                tflops=fl / t_pick / 1e9 if t_pick else 0.0,
+                tflops_best=fl / t_best / 1e9 if t_best else 0.0)
+
+
 # ---------------------------------------------------------------- dataset
 def generate(n=2000, seed=4, out="tune_random.npz", reps=1, start=0, checkpoint=100,
              max_elem=1 << 21, max_blocks=20000, max_flops=2e9, log=print):
@@ -257,6 +324,11 @@ def save(recs, path, meta):
         err=np.array([r.err for r in recs], np.float64),
         candidates=np.array([describe(c) for c in CANDIDATES]),
         meta=np.array([repr(meta)]))
+
+
+def held_out_specs(path=HELD_OUT):
+    with open(path) as f:
+        return json.load(f)
 
 
 def load_records(path):

@@ -322,7 +322,7 @@ __device__ __forceinline__ int oz_to_int(float x, float scale) {
 
 struct OzTile {
   const OzJob *J;
-  int64_t o, mt, nt, m, n, i0, j0, seg0, seg1, ksum;
+  int64_t o, mt, nt, m, n, i0, j0, seg0, seg1, ksum, c_off, erow, ecol;
   int32_t ga, gb, nmma;
 };
 
@@ -351,6 +351,47 @@ __device__ __forceinline__ void oz_decode(const OzLaunch &L, int64_t t, OzTile &
   T.gb = (int32_t)((rb + 7) / 8);
   T.nmma = (int32_t)(16 * ((rb + 15) / 16));
   T.ksum = J.ksum[T.o];
+}
+
+// The tile table of a launch (built once per batch).
+template <int N>
+__global__ void oz_table_kernel(OzLaunch L, OzTileRec *out) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= L.n_tiles) return;
+  OzTile T;
+  oz_decode<N>(L, t, T);
+  const OzJob &J = *T.J;
+  OzTileRec r;
+  r.seg0 = T.seg0;
+  r.seg1 = T.seg1;
+  r.ksum = T.ksum;
+  r.c_off = J.g.c_off[T.o];
+  r.m = T.m;
+  r.n = T.n;
+  r.erow = J.rowA[J.keyA[T.i0]];
+  r.ecol = J.rowB[J.keyB[T.j0]];
+  r.job = (int32_t)(T.J - L.jobs);
+  r.mt = (int32_t)T.mt;
+  r.nt = (int32_t)T.nt;
+  r.packed = T.ga | (T.gb << 8) | (T.nmma << 16);
+  out[t] = r;
+}
+
+__device__ __forceinline__ void oz_unpack(const OzLaunch &L, const OzTileRec &r, OzTile &T) {
+  T.J = L.jobs + r.job;
+  T.seg0 = r.seg0;
+  T.seg1 = r.seg1;
+  T.ksum = r.ksum;
+  T.c_off = r.c_off;
+  T.m = r.m;
+  T.n = r.n;
+  T.erow = r.erow;
+  T.ecol = r.ecol;
+  T.mt = r.mt;
+  T.nt = r.nt;
+  T.ga = r.packed & 0xff;
+  T.gb = (r.packed >> 8) & 0xff;
+  T.nmma = r.packed >> 16;
 }
 
 template <int N>
@@ -390,9 +431,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
     // ---------------- producer: one bulk copy per operand per k-step
     if (lane == 0) {
       uint32_t it = 0;
+      // the next tile's record is loaded one tile ahead
+      OzTileRec nxt;
+      if (blockIdx.x < L.n_tiles) nxt = L.tiles[blockIdx.x];
       for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
+        const OzTileRec cur = nxt;
+        if (t + gridDim.x < L.n_tiles) nxt = L.tiles[t + gridDim.x];
         OzTile T;
-        oz_decode<N>(L, t, T);
+        oz_unpack(L, cur, T);
         // job fields in registers: the asm memory clobbers below would reload them
         const OzJob &J = *T.J;
         const int s = J.s;
@@ -440,9 +486,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       for (int a = 0; a < OZ_NACC; a++) map |= (uint32_t)a << (3 * a);
 #pragma unroll
       for (int q = 0; q < NFREE; q++) fifo |= (uint32_t)(OZ_NACC + q) << (3 * q);
+      // the next tile's record is loaded one tile ahead
+      OzTileRec nxt;
+      if (blockIdx.x < L.n_tiles) nxt = L.tiles[blockIdx.x];
       for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
+        const OzTileRec cur = nxt;
+        if (t + gridDim.x < L.n_tiles) nxt = L.tiles[t + gridDim.x];
         OzTile T;
-        oz_decode<N>(L, t, T);
+        oz_unpack(L, cur, T);
         const OzJob &J = *T.J;
         const int s = J.s;
         const int n_acc = s < OZ_NACC ? s : OZ_NACC;
@@ -532,12 +583,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
     for (int q = 0; q < NFREE; q++) fifo |= (uint32_t)(OZ_NACC + q) << (3 * q);
     for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
       OzTile T;
-      oz_decode<N>(L, t, T);
+      oz_unpack(L, L.tiles[t], T);
       const OzJob &J = *T.J;
       const int n_acc = J.s < OZ_NACC ? J.s : OZ_NACC;
       const int64_t grow = T.mt * OZ_M + row;
       const bool row_ok = grow < T.m;
-      const int er = row_ok ? J.expA[J.rowA[J.keyA[T.i0]] + grow] : 0;
+      const int er = row_ok ? J.expA[T.erow + grow] : 0;
       // S: running sum in units of 2^-u of the leading slice product.  With
       // u <= 48 - log2(K) the sum stays below 2^62.1 for any data, and u >= 24
       // keeps D0..D2 (whole multiples of 2^-16) exact.
@@ -592,8 +643,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       }
       if (abort_flag) break;
       // C = S * 2^(e_r + f_c - 16 - u)
-      double *C = (double *)J.g.C + J.g.c_off[T.o];
-      const int64_t rowB = J.rowB[J.keyB[T.j0]];
+      double *C = (double *)J.g.C + T.c_off;
+      const int64_t rowB = T.ecol;
       const int32_t *expB = J.expB;
       if (row_ok) {
 #pragma unroll
@@ -673,6 +724,18 @@ tq_status oz_batch_build(const std::vector<OzJob> &jobs, const std::vector<OzSid
   L.tile_n = tile_n;
   L.nstages = oz_stages(s_max, tile_n);
   L.err = out.err.p;
+  TQ_CHECK(out.tiles.alloc(std::max<int64_t>(L.n_tiles, 1), st));
+  L.tiles = out.tiles.p;
+  if (L.n_tiles) {
+    const unsigned g = (unsigned)((L.n_tiles + 255) / 256);
+    count_launch();
+    switch (tile_n) {
+      case 32: oz_table_kernel<32><<<g, 256, 0, st>>>(L, out.tiles.p); break;
+      case 64: oz_table_kernel<64><<<g, 256, 0, st>>>(L, out.tiles.p); break;
+      default: oz_table_kernel<96><<<g, 256, 0, st>>>(L, out.tiles.p); break;
+    }
+    TQ_CUDA(cudaGetLastError());
+  }
   return TQ_OK;
 }
 

@@ -49,6 +49,18 @@ struct OzJob {
   int32_t tile_n;             // output columns per tile (every job of a launch alike)
 };
 
+// One output tile of a launch, decoded once when the launch is built: the GEMM's
+// three roles read it with one load instead of a chain of dependent lookups.
+struct __align__(16) OzTileRec {
+  int64_t seg0, seg1;   // pairs of the tile's output block (positions in the pair order)
+  int64_t ksum;         // k-steps of 16 over those pairs
+  int64_t c_off;        // offset of the output block in C
+  int64_t m, n;         // rows and columns of the output block
+  int64_t erow, ecol;   // first row / column of the block in the exponent tables
+  int32_t job, mt, nt;  // job index, row tile, column tile
+  int32_t packed;       // ga | gb << 8 | nmma << 16 (row groups of A and B, MMA width)
+};
+
 // Kernel parameter of a batched launch (arrays in device memory).
 struct OzLaunch {
   const OzJob *jobs;
@@ -63,6 +75,7 @@ struct OzLaunch {
   int64_t n_rows, n_slice_tiles, n_exps;
   int32_t s_max, nstages, tile_n;
   int32_t *err;
+  const OzTileRec *tiles;  // [n_tiles]
 };
 
 // Device copies of the job and side lists plus their prefix sums.
@@ -71,6 +84,7 @@ struct OzBatchDev {
   DevArray<OzSide> sides;
   DevArray<int64_t> prefixes;  // job tiles | side rows | side tiles | side exps
   DevArray<int32_t> err;
+  DevArray<OzTileRec> tiles;
   OzLaunch L{};
   int sms = 0;  // multiprocessors of the device: the persistent grid
 };

@@ -170,6 +170,22 @@ class RandomContraction:
     pairs: np.ndarray
     a_legs: list
     b_legs: list
+    legs_A: list = None  # sectors.Leg per leg of A
+    legs_B: list = None
+
+    def spec(self) -> dict:
+        """JSON-ready description (rebuild with from_spec)."""
+        leg = lambda l: [l.charges, l.sizes, l.direction]
+        return {"index": self.index, "A": [leg(l) for l in self.legs_A],
+                "B": [leg(l) for l in self.legs_B], "pairs": self.pairs.tolist()}
+
+
+def from_spec(d: dict) -> RandomContraction:
+    la = [Leg(*x) for x in d["A"]]
+    lb = [Leg(*x) for x in d["B"]]
+    pairs = np.asarray(d["pairs"], np.int64).reshape(-1, 2)
+    return RandomContraction(int(d["index"]), charge_blocks(la), charge_blocks(lb), pairs,
+                             pairs[:, 0].tolist(), pairs[:, 1].tolist(), la, lb)
 
 
 def _profile_sizes(dim: int, n: int, gaussian: bool):
@@ -270,6 +286,6 @@ def random_contractions(n: int = 2000, seed: int = 4, max_elem: int = 1 << 22,
             i += 1
             continue
         if pair_stats(A, B, pairs)[0] > 0:
-            out.append(RandomContraction(i, A, B, pairs, a_legs, b_legs))
+            out.append(RandomContraction(i, A, B, pairs, a_legs, b_legs, a_order, b_order))
         i += 1
     return out
