@@ -501,6 +501,9 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   J.expB = P->expB.p;
   J.s = sl;
   J.tile_n = tn;
+  TQ_CHECK(P->pair_tab.alloc(std::max<int64_t>(np, 1), s));
+  J.prs = P->pair_tab.p;
+  TQ_CHECK(oz_pair_table(J, np, P->pair_tab.p, s));
   return oz_batch_build({J}, {P->tc_side[0], P->tc_side[1]}, s, P->tcb);
 }
 

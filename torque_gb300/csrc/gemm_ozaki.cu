@@ -377,6 +377,29 @@ __global__ void oz_table_kernel(OzLaunch L, OzTileRec *out) {
   out[t] = r;
 }
 
+// The pair table of one job (built when its plan is made).
+__global__ void oz_pair_table_kernel(const int64_t *perm, const int32_t *pa, const int32_t *pb,
+                                     const int64_t *unitA, const int64_t *unitB,
+                                     const int32_t *nk_pair, int64_t n, OzPairRec *out) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int64_t p = perm ? perm[q] : q;
+  OzPairRec r;
+  r.a_off = 256 * unitA[pa[p]];
+  r.b_off = 256 * unitB[pb[p]];
+  r.nk = nk_pair[p];
+  r.pad = 0;
+  out[q] = r;
+}
+
+tq_status oz_pair_table(const OzJob &J, int64_t n_pairs, OzPairRec *out, cudaStream_t st) {
+  if (n_pairs == 0) return TQ_OK;
+  count_launch(), oz_pair_table_kernel<<<(unsigned)((n_pairs + 255) / 256), 256, 0, st>>>(
+      J.g.perm, J.g.pa, J.g.pb, J.unitA, J.unitB, J.nk_pair, n_pairs, out);
+  TQ_CUDA(cudaGetLastError());
+  return TQ_OK;
+}
+
 __device__ __forceinline__ void oz_unpack(const OzLaunch &L, const OzTileRec &r, OzTile &T) {
   T.J = L.jobs + r.job;
   T.seg0 = r.seg0;
@@ -442,16 +465,17 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         // job fields in registers: the asm memory clobbers below would reload them
         const OzJob &J = *T.J;
         const int s = J.s;
-        const int64_t *perm = J.g.perm, *unitA = J.unitA, *unitB = J.unitB;
-        const int32_t *pa = J.g.pa, *pb = J.g.pb, *nk_pair = J.nk_pair;
+        const OzPairRec *prs = J.prs;
         const uint8_t *sliceA = J.sliceA, *sliceB = J.sliceB;
         const uint32_t ba = (uint32_t)s * T.ga * 256, bb = (uint32_t)s * T.gb * 256;
+        // the next pair's record is loaded one pair ahead
+        OzPairRec pn = prs[T.seg0];
         for (int64_t sidx = T.seg0; sidx < T.seg1 && !abort_flag; sidx++) {
-          const int64_t p = perm ? perm[sidx] : sidx;
-          const int64_t i = pa[p], j = pb[p];
-          const int64_t nk = nk_pair[p];
-          const uint8_t *ga = sliceA + 256 * unitA[i] + nk * s * 256 * (OZ_M / 8) * T.mt;
-          const uint8_t *gb = sliceB + 256 * unitB[j] + nk * s * 256 * (N / 8) * T.nt;
+          const OzPairRec pr = pn;
+          if (sidx + 1 < T.seg1) pn = prs[sidx + 1];
+          const int64_t nk = pr.nk;
+          const uint8_t *ga = sliceA + pr.a_off + nk * s * 256 * (OZ_M / 8) * T.mt;
+          const uint8_t *gb = sliceB + pr.b_off + nk * s * 256 * (N / 8) * T.nt;
           for (int64_t q = 0; q < nk; q++, it++) {
             const uint32_t st = it % NS, use = it / NS;
             if (use > 0 && !mbar_wait(&empty_bar[st], (use - 1) & 1)) {
@@ -497,8 +521,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         const OzJob &J = *T.J;
         const int s = J.s;
         const int n_acc = s < OZ_NACC ? s : OZ_NACC;
-        const int64_t *perm = J.g.perm;
-        const int32_t *nk_pair = J.nk_pair;
+        const OzPairRec *prs = J.prs;
         const uint32_t idesc = idesc_bf16_f32(OZ_M, (uint32_t)T.nmma);
         OzSchedule sch;
         sch.start(T.ksum, n_acc);
@@ -507,9 +530,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         sch.peek(ev_k, ev_kind);
         uint32_t fresh = (1u << n_acc) - 1;  // accumulators to (re)start in a free slot
         int64_t k = 0;
+        int32_t nk_next = prs[T.seg0].nk;
         for (int64_t sidx = T.seg0; sidx < T.seg1 && !abort_flag; sidx++) {
-          const int64_t p = perm ? perm[sidx] : sidx;
-          const int64_t nk = nk_pair[p];
+          const int64_t nk = nk_next;
+          if (sidx + 1 < T.seg1) nk_next = prs[sidx + 1].nk;
           for (int64_t q = 0; q < nk; q++, it++) {
             const uint32_t st = it % NS, use = it / NS;
             if (!mbar_wait(&full_bar[st], use & 1)) {

@@ -34,8 +34,17 @@ struct OzSide {
   int32_t s, rt_rows;
 };
 
+// One block pair of a job, in the order the GEMM walks them (pairs of each
+// output block consecutive): byte offsets of the two blocks' slices and the
+// pair's k-steps of 16.
+struct __align__(8) OzPairRec {
+  int64_t a_off, b_off;
+  int32_t nk, pad;
+};
+
 struct OzJob {
   GemmJob g;
+  const OzPairRec *prs;       // [n_pairs] by position in the pair order (seg)
   const int64_t *tile_start;  // [n_out+1] first 128x96 tile of output o
   int64_t n_tiles;
   const int64_t *ksum;        // per output: k-steps of 16 over its pairs
@@ -90,6 +99,8 @@ struct OzBatchDev {
 };
 
 int oz_stages(int s, int tile_n);
+// The pair table of job J (J's pair arrays, unit offsets and k-steps made).
+tq_status oz_pair_table(const OzJob &J, int64_t n_pairs, OzPairRec *out, cudaStream_t st);
 tq_status oz_batch_build(const std::vector<OzJob> &jobs, const std::vector<OzSide> &sides,
                          cudaStream_t s, OzBatchDev &out);
 // Row exponents and slices of every side of the batch.

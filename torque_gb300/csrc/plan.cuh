@@ -51,6 +51,7 @@ struct tq_plan {
   tq::DevArray<int64_t> hyb_tile_start;
   int64_t hyb_tiles = 0;
   tq::NativeWorkDev hyb;
+  tq::DevArray<tq::OzPairRec> pair_tab;  // pairs in GEMM order (tensor-core forms)
   tq::OzJob tc_job{};              // this contraction as one job
   tq::OzSide tc_side[2]{};         // its A and B operand sides
   tq::OzBatchDev tcb;              // the same as a batch of one, on the device
