@@ -251,7 +251,7 @@ static_assert(OZ_STAG * (OZ_NACC - 1) < OZ_CHUNK, "stagger must fit one chunk");
 // by whole row groups (the start-address field counts 16-byte units).  The first
 // product of the k-step into an accumulator whose bit is set in `fresh`
 // overwrites it.
-template <int S>
+template <int S, bool FRESH>
 __device__ __forceinline__ void oz_issue(const uint32_t (&col)[OZ_NACC], uint64_t da0,
                                          uint64_t db0, uint32_t a_step, uint32_t b_step,
                                          uint32_t idesc, uint32_t fresh) {
@@ -262,23 +262,24 @@ __device__ __forceinline__ void oz_issue(const uint32_t (&col)[OZ_NACC], uint64_
       const int acc = t + u < OZ_NACC - 1 ? t + u : OZ_NACC - 1;
       // first (t, u) in this order that lands in accumulator acc
       const bool first = acc < OZ_NACC - 1 ? t == 0 : (t == 0 && u == OZ_NACC - 1);
-      const uint32_t keep = (first && ((fresh >> acc) & 1)) ? 0u : 1u;
+      const uint32_t keep = (FRESH && first && ((fresh >> acc) & 1)) ? 0u : 1u;
       mma_bf16(col[acc], da0 + (uint64_t)(t * a_step), db0 + (uint64_t)(u * b_step), idesc, keep);
     }
   }
 }
 
+template <bool FRESH>
 __device__ __forceinline__ void oz_issue_s(int s, const uint32_t (&col)[OZ_NACC], uint64_t da0,
                                            uint64_t db0, uint32_t a_step, uint32_t b_step,
                                            uint32_t idesc, uint32_t fresh) {
   switch (s) {
-    case 1: oz_issue<1>(col, da0, db0, a_step, b_step, idesc, fresh); break;
-    case 2: oz_issue<2>(col, da0, db0, a_step, b_step, idesc, fresh); break;
-    case 3: oz_issue<3>(col, da0, db0, a_step, b_step, idesc, fresh); break;
-    case 4: oz_issue<4>(col, da0, db0, a_step, b_step, idesc, fresh); break;
-    case 5: oz_issue<5>(col, da0, db0, a_step, b_step, idesc, fresh); break;
-    case 6: oz_issue<6>(col, da0, db0, a_step, b_step, idesc, fresh); break;
-    default: oz_issue<7>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    case 1: oz_issue<1, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    case 2: oz_issue<2, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    case 3: oz_issue<3, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    case 4: oz_issue<4, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    case 5: oz_issue<5, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    case 6: oz_issue<6, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    default: oz_issue<7, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
   }
 }
 
@@ -454,6 +455,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
     // ---------------- producer: one bulk copy per operand per k-step
     if (lane == 0) {
       uint32_t it = 0;
+      // stage of k-step `it` and the parity of its previous use (counters, not it % NS)
+      uint32_t st = 0, ph = 1;
       // the next tile's record is loaded one tile ahead
       OzTileRec nxt;
       if (blockIdx.x < L.n_tiles) nxt = L.tiles[blockIdx.x];
@@ -477,8 +480,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
           const uint8_t *ga = sliceA + pr.a_off + nk * s * 256 * (OZ_M / 8) * T.mt;
           const uint8_t *gb = sliceB + pr.b_off + nk * s * 256 * (N / 8) * T.nt;
           for (int64_t q = 0; q < nk; q++, it++) {
-            const uint32_t st = it % NS, use = it / NS;
-            if (use > 0 && !mbar_wait(&empty_bar[st], (use - 1) & 1)) {
+            if (it >= (uint32_t)NS && !mbar_wait(&empty_bar[st], ph)) {
               atomicOr(L.err, 1);
               abort_flag = 1;
               break;
@@ -487,6 +489,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
             mbar_arrive_expect_tx(&full_bar[st], ba + bb);
             bulk_g2s(sa, ga + q * ba, ba, &full_bar[st]);
             bulk_g2s(sa + a_bytes_max, gb + q * bb, bb, &full_bar[st]);
+            if (++st == (uint32_t)NS) {
+              st = 0;
+              ph ^= 1;
+            }
           }
         }
       }
@@ -500,6 +506,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
     // ---------------- MMA issuer
     if (lane == 0) {
       uint32_t it = 0;
+      uint32_t st = 0, ph = 0;  // stage of k-step `it` and its fill parity
+      // smem descriptors of stage 0; a stage's are these plus its offset / 16
+      const uint32_t sm0 = smem_u32(smem);
+      const uint64_t dA0 = smem_desc(sm0, 128, 256), dB0 = smem_desc(sm0 + a_bytes_max, 128, 256);
       // slot of accumulator a in bits [3a, 3a+3); per slot p: bit p of `par` is
       // the parity of its completed uses, bit p of `used` whether it had one
       uint32_t map = 0, par = 0, used = 0;
@@ -530,39 +540,44 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         sch.peek(ev_k, ev_kind);
         uint32_t fresh = (1u << n_acc) - 1;  // accumulators to (re)start in a free slot
         int64_t k = 0;
+        uint32_t col[OZ_NACC];
+#pragma unroll
+        for (int a = 0; a < OZ_NACC; a++) col[a] = tmem + ((map >> (3 * a)) & 7) * N;
         int32_t nk_next = prs[T.seg0].nk;
         for (int64_t sidx = T.seg0; sidx < T.seg1 && !abort_flag; sidx++) {
           const int64_t nk = nk_next;
           if (sidx + 1 < T.seg1) nk_next = prs[sidx + 1].nk;
           for (int64_t q = 0; q < nk; q++, it++) {
-            const uint32_t st = it % NS, use = it / NS;
-            if (!mbar_wait(&full_bar[st], use & 1)) {
+            if (!mbar_wait(&full_bar[st], ph)) {
               atomicOr(L.err, 4);
               abort_flag = 1;
               break;
             }
-            // a slot taken up again must have been drained since its last use
-            bool ok = true;
+            if (fresh) {
+              // a slot taken up again must have been drained since its last use
+              bool ok = true;
 #pragma unroll
-            for (int a = 0; a < OZ_NACC; a++) {
-              const uint32_t p = (map >> (3 * a)) & 7;
-              if (((fresh >> a) & 1) && ((used >> p) & 1) &&
-                  !mbar_wait(&slot_empty[p], ((par >> p) & 1) ^ 1))
-                ok = false;
-            }
-            if (!ok) {
-              atomicOr(L.err, 8);
-              abort_flag = 1;
-              break;
+              for (int a = 0; a < OZ_NACC; a++) {
+                const uint32_t p = (map >> (3 * a)) & 7;
+                if (((fresh >> a) & 1) && ((used >> p) & 1) &&
+                    !mbar_wait(&slot_empty[p], ((par >> p) & 1) ^ 1))
+                  ok = false;
+              }
+              if (!ok) {
+                atomicOr(L.err, 8);
+                abort_flag = 1;
+                break;
+              }
             }
             tc_fence_after();
-            uint32_t col[OZ_NACC];
-#pragma unroll
-            for (int a = 0; a < OZ_NACC; a++) col[a] = tmem + ((map >> (3 * a)) & 7) * N;
-            const uint32_t sa = smem_u32(smem + st * stage_bytes);
-            oz_issue_s(s, col, smem_desc(sa, 128, 256), smem_desc(sa + a_bytes_max, 128, 256),
-                       (uint32_t)T.ga * 16, (uint32_t)T.gb * 16, idesc, fresh);
+            const uint64_t so = (uint64_t)((st * stage_bytes) >> 4);
+            oz_issue_s<true>(s, col, dA0 + so, dB0 + so, (uint32_t)T.ga * 16, (uint32_t)T.gb * 16,
+                             idesc, fresh);
             mma_commit(&empty_bar[st]);
+            if (++st == (uint32_t)NS) {
+              st = 0;
+              ph ^= 1;
+            }
             fresh = 0;
             if (++k == ev_k) {
 #pragma unroll
@@ -576,6 +591,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
                 const uint32_t q = fifo & 7;
                 fifo = (fifo >> 3) | (p << (3 * (NFREE - 1)));
                 map = (map & ~(7u << (3 * a))) | (q << (3 * a));
+                col[a] = tmem + q * N;
                 fresh |= 1u << a;
               }
               if (ev_kind != OZ_FINAL) {
