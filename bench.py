@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--no-sweep", action="store_true")
     p.add_argument("--no-peps", action="store_true")
     p.add_argument("--no-tune", action="store_true")
+    p.add_argument("--no-hbm", action="store_true")
     p.add_argument("--no-costmodel", action="store_true")
     return p.parse_args()
 
@@ -396,6 +397,8 @@ def run_ours(args):
 
         if not args.no_fp64:
             line["plain_fp64"] = fp64_subset(tq, c, A, a, b, kw)
+        if not args.no_hbm:
+            line["hbm_kernels"] = hbm_kernels(tq, c, A, B)
         if not args.no_sweep:
             line["batched_sweep"] = sweep(tq)
         if not args.no_peps:
@@ -419,6 +422,44 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def hbm_kernels(tq, c, A, B):
+    """The bandwidth-bound kernels on the full tensors: hard_transpose of A
+    (21.5 GB read + written) for a leg-0-moving and a leg-0-keeping permutation,
+    as GB/s of algorithmic traffic (read + write of every element) against the
+    measured copy bandwidth; and the symbolic stage (pair matching over
+    23,969 x 23,969 blocks, output boxes, the reduced layout's sort) as time."""
+    import torch
+    pk = measured_peaks()
+    out = {"hbm_peak_gbs": pk["hbm_gbs"], "peak_source": pk["source"] + " copy"}
+    nbytes = 2 * 8 * c.A.n_elem
+    for name, perm in (("transpose_1032", [1, 0, 3, 2]), ("transpose_0213", [0, 2, 1, 3])):
+        T = A.hard_transpose(perm)  # warm-up (plans its tiles, allocates)
+        del T
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(3):
+            t = time.perf_counter()
+            T = A.hard_transpose(perm)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t)
+            del T
+        dt = min(ts)
+        out[name] = {"ms": dt * 1e3, "gbs": nbytes / dt / 1e9, "frac": nbytes / dt / 1e9 / pk["hbm_gbs"],
+                     "bytes": nbytes, "timing": "wall time of tq_bs_hard_transpose incl. its "
+                     "tile planning (one host sync), best of 3"}
+    ts = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        P = tq.ContractionPlan(A, B, c.pairs, layout="reduced")
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t)
+        del P
+    out["symbolic_stage_ms"] = min(ts) * 1e3
+    out["interval_tests"] = float(c.A.n_blocks) * float(c.B.n_blocks)
+    return out
 
 
 def tune_name(c):

@@ -96,7 +96,8 @@ def test_non_adjacent_free_legs(tq, small):
         check_reference_layout(tq, A, B, hA, hB, np.array(pairs))
 
 
-@pytest.mark.parametrize("perm", [[1, 0, 2, 3], [3, 2, 1, 0], [0, 1, 3, 2], [2, 0, 3, 1]])
+@pytest.mark.parametrize("perm", [[1, 0, 2, 3], [3, 2, 1, 0], [0, 1, 3, 2], [2, 0, 3, 1],
+                                  [0, 2, 3, 1], [0, 1, 2, 3]])
 def test_hard_transpose_bit_exact(tq, small, perm):
     c = small
     A = to_gpu(tq, c.A.dimension, c.A.begin, c.A.end, c.a_data)
@@ -105,6 +106,22 @@ def test_hard_transpose_bit_exact(tq, small, perm):
     want = orc.hard_transpose(hA, perm)
     dim, b, e, t, o = T.metadata()
     assert np.array_equal(dim, want.dimension)
+    assert np.array_equal(b.T, want.begin) and np.array_equal(e.T, want.end)
+    assert np.array_equal(T.data(), want.data)
+
+
+@pytest.mark.parametrize("perm", [[0, 2, 1], [1, 0, 2], [2, 1, 0], [0, 1, 2]])
+def test_hard_transpose_long_legs(tq, perm):
+    """Blocks longer than one 32-wide tile on every leg (several tiles per
+    block on both transposed legs, ragged edges), bit-exact with the oracle."""
+    from torque_gb300.sectors import Leg, charge_blocks
+    legs = [Leg([0, 1], [37, 70], 1), Leg([0, 1], [33, 5], -1), Leg([0, 1], [3, 41], 1)]
+    bl = charge_blocks(legs, 0, modulus=2)
+    data = np.random.default_rng(8).standard_normal(bl.n_elem)
+    A = to_gpu(tq, bl.dimension, bl.begin, bl.end, data)
+    want = orc.hard_transpose(host(bl.dimension, bl.begin, bl.end, data), perm)
+    T = A.hard_transpose(perm)
+    dim, b, e, t, o = T.metadata()
     assert np.array_equal(b.T, want.begin) and np.array_equal(e.T, want.end)
     assert np.array_equal(T.data(), want.data)
 

@@ -6,8 +6,8 @@
 // n_blocks).  Here every block is permuted in place of its own extent: a work
 // list of 32x32 tiles spanning (input leg 0) x (output leg 0), batched over the
 // other legs, staged through shared memory so that both the reads and the
-// writes run along the unit-stride leg.  When leg 0 stays leg 0 the tile is a
-// straight copy of contiguous runs.
+// writes run along the unit-stride leg.  When leg 0 stays leg 0 a tile is 8
+// straight copies of contiguous runs, one per warp.
 #include <cstring>
 
 #include "index.cuh"
@@ -22,46 +22,44 @@ struct TransposeJob {
   int32_t rank;
   int32_t perm[TQ_MAXR];
   const int64_t *out_off;     // output block offsets
-  const int64_t *tile_start;  // [nb+1]
+  const int64_t *tile_start;  // [nb] first tile of each block
+  const int32_t *tile_block;  // [n_tiles] block of each tile
   int64_t nb;
   void *out;
 };
 
-__device__ __forceinline__ int64_t find_block(const int64_t *start, int64_t n, int64_t t) {
-  int64_t lo = 0, hi = n - 1;
-  while (lo < hi) {
-    const int64_t mid = (lo + hi + 1) >> 1;
-    if (start[mid] <= t) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
-// Tiles of block b: ceil(d_in0/32) * ceil(d_out0/32) * prod(other dims), where
-// d_in0 = dim of input leg 0 and d_out0 = dim of input leg perm[0].
+// Tiles of block b.  Transposing (leg 0 moves): ceil(d_in0/32) * ceil(d_out0/32)
+// * prod(other dims), d_out0 = dim of input leg perm[0], 32x32 tiles through
+// shared memory.  Leg 0 stays: ceil(d_0/32) * ceil(prod(other dims)/8), each
+// tile 8 runs of up to 32 contiguous elements (one warp per run).
 __global__ void transpose_tiles_kernel(DevBS in, int32_t p0, int64_t *tiles) {
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= in.nb) return;
   const int64_t *bb = in.begin + b * in.rank, *be = in.end + b * in.rank;
-  int64_t n = 1;
+  int64_t n = 1, rest = 1;
   for (int l = 0; l < in.rank; l++) {
     const int64_t d = be[l] - bb[l] + 1;
     if (l == 0 || l == p0) n *= (d + TT - 1) / TT;
-    else n *= d;
+    else rest *= d;
   }
-  tiles[b] = in.rank ? n : 0;
+  tiles[b] = !in.rank ? 0 : p0 == 0 ? n * ((rest + 7) / 8) : n * rest;
+}
+
+// block of every tile (one load per CTA instead of a search)
+__global__ void tile_block_kernel(const int64_t *tile_start, int64_t nb, int64_t n_tiles,
+                                  int32_t *tile_block) {
+  const int64_t b = (int64_t)blockIdx.x;
+  if (b >= nb) return;
+  const int64_t t0 = tile_start[b], t1 = b + 1 < nb ? tile_start[b + 1] : n_tiles;
+  for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) tile_block[t] = (int32_t)b;
 }
 
 template <typename T>
 __global__ void __launch_bounds__(256) transpose_kernel(TransposeJob job) {
   __shared__ T tile[TT][TT + 1];
-  __shared__ int64_t s_b, s_local;
   const int64_t t = blockIdx.x;
-  if (threadIdx.x == 0) {
-    s_b = find_block(job.tile_start, job.nb, t);
-    s_local = t - job.tile_start[s_b];
-  }
-  __syncthreads();
-  const int64_t b = s_b;
+  const int64_t b = job.tile_block[t];
+  const int64_t local = t - job.tile_start[b];
   const int r = job.rank;
   const int32_t p0 = job.perm[0];
   const int64_t *bb = job.in.begin + b * r, *be = job.in.end + b * r;
@@ -77,17 +75,30 @@ __global__ void __launch_bounds__(256) transpose_kernel(TransposeJob job) {
       s *= d[job.perm[q]];
     }
   }
-  // decode the tile: leg 0 tile, leg p0 tile, then the other legs
-  int64_t x = s_local;
+  const T *src = (const T *)job.in.data;
+  T *dst = (T *)job.out;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
   const int64_t n0 = (d[0] + TT - 1) / TT;
-  const int64_t i0 = (x % n0) * TT;
-  x /= n0;
-  int64_t j0 = 0;
-  if (p0 != 0) {
-    const int64_t np = (d[p0] + TT - 1) / TT;
-    j0 = (x % np) * TT;
-    x /= np;
+  const int64_t i0 = (local % n0) * TT;
+  int64_t x = local / n0;
+  if (p0 == 0) {
+    // leg 0 stays fastest: warp ty copies the run of row 8*x + ty (the other
+    // legs in input order, leg 1 fastest), up to 32 elements of leg 0
+    int64_t row = 8 * x + ty, in_base = job.in.offsets[b], out_base = job.out_off[b];
+    for (int l = 1; l < r; l++) {
+      const int64_t c = row % d[l];
+      row /= d[l];
+      in_base += c * st[l];
+      out_base += c * ost[l];
+    }
+    if (row == 0 && i0 + tx < d[0])
+      dst[out_base + (i0 + tx) * ost[0]] = src[in_base + (i0 + tx) * st[0]];
+    return;
   }
+  // decode the rest of the tile: leg p0 tile, then the other legs
+  const int64_t np = (d[p0] + TT - 1) / TT;
+  const int64_t j0 = (x % np) * TT;
+  x /= np;
   int64_t in_base = job.in.offsets[b], out_base = job.out_off[b];
   for (int l = 1; l < r; l++) {
     if (l == p0) continue;
@@ -95,15 +106,6 @@ __global__ void __launch_bounds__(256) transpose_kernel(TransposeJob job) {
     x /= d[l];
     in_base += c * st[l];
     out_base += c * ost[l];
-  }
-  const T *src = (const T *)job.in.data;
-  T *dst = (T *)job.out;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
-  if (p0 == 0) {
-    // leg 0 stays fastest: copy up to 32 contiguous elements of leg 0
-    if (ty == 0 && i0 + tx < d[0])
-      dst[out_base + (i0 + tx) * ost[0]] = src[in_base + (i0 + tx) * st[0]];
-    return;
   }
   // read along input leg 0, write along output leg 0 (= input leg p0)
   for (int q = ty; q < TT; q += 8) {
@@ -170,6 +172,7 @@ extern "C" tq_status tq_bs_hard_transpose(const tq_bs *t, const int64_t *perm, t
   TQ_CHECK(sync_device_meta(o, s));
   if (t->nb) {
     DevArray<int64_t> tiles, tile_start, total;
+    DevArray<int32_t> tile_block;
     TQ_CHECK(tiles.alloc(t->nb, s));
     TQ_CHECK(tile_start.alloc(t->nb, s));
     TQ_CHECK(total.alloc(1, s));
@@ -189,7 +192,12 @@ extern "C" tq_status tq_bs_hard_transpose(const tq_bs *t, const int64_t *perm, t
     job.nb = t->nb;
     job.out = o->data;
     if (n_tiles > 0x7fffffffLL) return fail(TQ_ERR_UNSUPPORTED, "more than 2^31 transpose tiles");
+    if (t->nb > 0x7fffffffLL) return fail(TQ_ERR_UNSUPPORTED, "more than 2^31 blocks");
+    TQ_CHECK(tile_block.alloc(std::max<int64_t>(n_tiles, 1), s));
+    job.tile_block = tile_block.p;
     if (n_tiles) {
+      count_launch(), tile_block_kernel<<<(unsigned)t->nb, 256, 0, s>>>(tile_start.p, t->nb, n_tiles,
+                                                                         tile_block.p);
       if (t->dtype == TQ_F64)
         count_launch(), transpose_kernel<double><<<(unsigned)n_tiles, 256, 0, s>>>(job);
       else
