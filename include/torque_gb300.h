@@ -299,6 +299,11 @@ tq_status tq_batch_destroy(tq_batch *batch);
 
 /* ---- errors and hooks -------------------------------------------------- */
 
+/* Device memory comes from the library's own stream-ordered pool per device,
+ * which keeps freed memory for reuse; this returns every unused byte of those
+ * pools to the driver (synchronises the devices that have one). */
+tq_status tq_release_cached_memory(void);
+
 /* Message of the last failing call on this thread. */
 const char *tq_last_error_string(void);
 

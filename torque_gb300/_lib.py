@@ -83,6 +83,7 @@ SIGNATURES = {
     "tq_batch_kernels": (ST, [P, P64]),
     "tq_batch_destroy": (ST, [P]),
     "tq_last_error_string": (ctypes.c_char_p, []),
+    "tq_release_cached_memory": (ST, []),
     "tq_debug_fail_alloc_after": (None, [I64]),
     "tq_debug_kernel_launches": (I64, []),
 }

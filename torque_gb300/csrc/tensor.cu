@@ -29,6 +29,35 @@ tq_status cuda_fail(cudaError_t e, const char *what) {
   return TQ_ERR_CUDA;
 }
 
+// The library's own stream-ordered memory pool per device.  Freed memory stays
+// in the pool (release threshold: unlimited), so a contraction that allocates
+// tens of GB again and again does not map and unmap pages every time; the
+// process's default pool is left as it was.  tq_release_cached_memory trims it.
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pools[128] = {nullptr};
+
+static tq_status device_pool(cudaMemPool_t *pool) {
+  int dev = 0;
+  TQ_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return fail(TQ_ERR_UNSUPPORTED, "device ordinal above 127");
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  if (!g_pools[dev]) {
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pl = nullptr;
+    TQ_CUDA(cudaMemPoolCreate(&pl, &props));
+    uint64_t keep = UINT64_MAX;
+    TQ_CUDA(cudaMemPoolSetAttribute(pl, cudaMemPoolAttrReleaseThreshold, &keep));
+    g_pools[dev] = pl;
+  }
+  *pool = g_pools[dev];
+  return TQ_OK;
+}
+
 tq_status dev_alloc(void **p, size_t bytes, cudaStream_t s) {
   *p = nullptr;
   int64_t b = g_alloc_budget.load();
@@ -37,10 +66,12 @@ tq_status dev_alloc(void **p, size_t bytes, cudaStream_t s) {
     g_alloc_budget.store(b - 1);
   }
   if (bytes == 0) bytes = 16;
-  cudaError_t e = cudaMallocAsync(p, bytes, s);
+  cudaMemPool_t pool = nullptr;
+  TQ_CHECK(device_pool(&pool));
+  cudaError_t e = cudaMallocFromPoolAsync(p, bytes, pool, s);
   if (e != cudaSuccess) {
     *p = nullptr;
-    return cuda_fail(e, "cudaMallocAsync");
+    return cuda_fail(e, "cudaMallocFromPoolAsync");
   }
   return TQ_OK;
 }
@@ -149,6 +180,22 @@ static tq_status append_meta(tq_bs *t, int64_t n, const int64_t *b, const int64_
 }  // namespace tq
 
 using namespace tq;
+
+extern "C" tq_status tq_release_cached_memory(void) {
+  std::lock_guard<std::mutex> lk(tq::g_pool_mu);
+  for (int d = 0; d < 128; d++) {
+    if (!tq::g_pools[d]) continue;
+    int cur = 0;
+    TQ_CUDA(cudaGetDevice(&cur));
+    TQ_CUDA(cudaSetDevice(d));
+    const cudaError_t e1 = cudaDeviceSynchronize();
+    const cudaError_t e2 = cudaMemPoolTrimTo(tq::g_pools[d], 0);
+    TQ_CUDA(cudaSetDevice(cur));
+    TQ_CUDA(e1);
+    TQ_CUDA(e2);
+  }
+  return TQ_OK;
+}
 
 extern "C" {
 

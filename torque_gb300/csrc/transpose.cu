@@ -3,11 +3,16 @@
 //
 // The reference packs all blocks into a stack padded to the global maximum
 // block dims, permutes it with cuTT and unpacks it (memory = max dims x
-// n_blocks).  Here every block is permuted in place of its own extent: a work
-// list of 32x32 tiles spanning (input leg 0) x (output leg 0), batched over the
-// other legs, staged through shared memory so that both the reads and the
-// writes run along the unit-stride leg.  When leg 0 stays leg 0 a tile is 8
-// straight copies of contiguous runs, one per warp.
+// n_blocks).  Here every block is permuted in place of its own extent.  The
+// unit of work is the "plane" of input leg 0 and the leg that becomes output
+// leg 0 (p0), for one combination of the other legs: contiguous in the input
+// along leg 0 and in the output along leg p0.  Sector-sized blocks have small
+// planes, so a tile batches up to 256 planes of up to PLANE_MAX elements: the
+// planes' base offsets are decoded once per plane into shared memory, the
+// elements are read along input leg 0 into a padded shared buffer and written
+// along output leg 0.  When leg 0 stays leg 0 a plane is a contiguous run and
+// is copied straight.  Planes too large for the buffer fall back to 32 x 32
+// tiles.  Tiles are walked by a persistent grid; one load finds a tile's block.
 #include <cstring>
 
 #include "index.cuh"
@@ -15,7 +20,9 @@
 
 namespace tq {
 
-constexpr int TT = 32;  // tile edge
+constexpr int TT = 32;            // edge of the large-plane tiles
+constexpr int PLANE_MAX = 4096;   // elements of the shared buffer
+constexpr int PLANES_MAX = 256;   // planes per tile
 
 struct TransposeJob {
   DevBS in;
@@ -28,24 +35,49 @@ struct TransposeJob {
   void *out;
 };
 
-// Tiles of block b.  Transposing (leg 0 moves): ceil(d_in0/32) * ceil(d_out0/32)
-// * prod(other dims), d_out0 = dim of input leg perm[0], 32x32 tiles through
-// shared memory.  Leg 0 stays: ceil(d_0/32) * ceil(prod(other dims)/8), each
-// tile 8 runs of up to 32 contiguous elements (one warp per run).
-__global__ void transpose_tiles_kernel(DevBS in, int32_t p0, int64_t *tiles) {
-  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= in.nb) return;
-  const int64_t *bb = in.begin + b * in.rank, *be = in.end + b * in.rank;
-  int64_t n = 1, rest = 1;
-  for (int l = 0; l < in.rank; l++) {
-    const int64_t d = be[l] - bb[l] + 1;
-    if (l == 0 || l == p0) n *= (d + TT - 1) / TT;
-    else rest *= d;
+// Tiling of one block (host and device agree through this one function).
+// mode 0: runs (p0 == 0), 1: batched planes, 2: 32 x 32 tiles.
+struct PlanePlan {
+  int mode;
+  uint32_t P;        // elements of a plane in the shared buffer (padded, mode 1)
+  uint32_t ppc;      // planes per tile (modes 0 and 1)
+  uint32_t rows;     // planes of the block (product of the other legs)
+  int64_t tiles;
+};
+
+__host__ __device__ inline PlanePlan plane_plan(const uint32_t *d, int r, int p0) {
+  PlanePlan pp;
+  uint64_t rows = 1;
+  for (int l = 1; l < r; l++)
+    if (l != p0) rows *= d[l];
+  pp.rows = (uint32_t)rows;
+  if (p0 == 0) {
+    pp.mode = 0;
+    pp.P = d[0];
+    uint32_t ppc = PLANE_MAX / (d[0] ? d[0] : 1);
+    ppc = ppc < 1 ? 1 : (ppc > PLANES_MAX ? PLANES_MAX : ppc);
+    pp.ppc = ppc;
+    pp.tiles = d[0] > (uint32_t)PLANE_MAX ? (int64_t)rows * ((d[0] + PLANE_MAX - 1) / PLANE_MAX)
+                                          : (int64_t)((rows + ppc - 1) / ppc);
+    return pp;
   }
-  tiles[b] = !in.rank ? 0 : p0 == 0 ? n * ((rest + 7) / 8) : n * rest;
+  const uint64_t P = (uint64_t)(d[0] + 1) * d[p0];  // leg-0 runs padded by one
+  if (P <= (uint64_t)PLANE_MAX) {
+    pp.mode = 1;
+    pp.P = (uint32_t)P;
+    uint32_t ppc = PLANE_MAX / pp.P;
+    pp.ppc = ppc > PLANES_MAX ? PLANES_MAX : ppc;
+    pp.tiles = (int64_t)((rows + pp.ppc - 1) / pp.ppc);
+    return pp;
+  }
+  pp.mode = 2;
+  pp.P = 0;
+  pp.ppc = 1;
+  pp.tiles = (int64_t)((d[0] + TT - 1) / TT) * ((d[p0] + TT - 1) / TT) * (int64_t)rows;
+  return pp;
 }
 
-// block of every tile (one load per CTA instead of a search)
+// block of every tile (one load per tile instead of a search)
 __global__ void tile_block_kernel(const int64_t *tile_start, int64_t nb, int64_t n_tiles,
                                   int32_t *tile_block) {
   const int64_t b = (int64_t)blockIdx.x;
@@ -54,68 +86,105 @@ __global__ void tile_block_kernel(const int64_t *tile_start, int64_t nb, int64_t
   for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) tile_block[t] = (int32_t)b;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) transpose_kernel(TransposeJob job) {
-  __shared__ T tile[TT][TT + 1];
-  const int64_t t = blockIdx.x;
-  const int64_t b = job.tile_block[t];
-  const int64_t local = t - job.tile_start[b];
-  const int r = job.rank;
-  const int32_t p0 = job.perm[0];
-  const int64_t *bb = job.in.begin + b * r, *be = job.in.end + b * r;
-  const int64_t *st = job.in.strides + b * r;
-  int64_t d[TQ_MAXR];
-  for (int l = 0; l < r; l++) d[l] = be[l] - bb[l] + 1;
-  // output strides: column-major over the permuted dims
-  int64_t ost[TQ_MAXR];  // stride in the output of INPUT leg l
-  {
-    int64_t s = 1;
-    for (int q = 0; q < r; q++) {
-      ost[job.perm[q]] = s;
-      s *= d[job.perm[q]];
-    }
-  }
-  const T *src = (const T *)job.in.data;
-  T *dst = (T *)job.out;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
-  const int64_t n0 = (d[0] + TT - 1) / TT;
-  const int64_t i0 = (local % n0) * TT;
-  int64_t x = local / n0;
-  if (p0 == 0) {
-    // leg 0 stays fastest: warp ty copies the run of row 8*x + ty (the other
-    // legs in input order, leg 1 fastest), up to 32 elements of leg 0
-    int64_t row = 8 * x + ty, in_base = job.in.offsets[b], out_base = job.out_off[b];
-    for (int l = 1; l < r; l++) {
-      const int64_t c = row % d[l];
-      row /= d[l];
-      in_base += c * st[l];
-      out_base += c * ost[l];
-    }
-    if (row == 0 && i0 + tx < d[0])
-      dst[out_base + (i0 + tx) * ost[0]] = src[in_base + (i0 + tx) * st[0]];
-    return;
-  }
-  // decode the rest of the tile: leg p0 tile, then the other legs
-  const int64_t np = (d[p0] + TT - 1) / TT;
-  const int64_t j0 = (x % np) * TT;
-  x /= np;
-  int64_t in_base = job.in.offsets[b], out_base = job.out_off[b];
+// Offsets in the input and the output of plane `row` (the other legs in input
+// order, lowest leg fastest).
+__device__ __forceinline__ void plane_bases(uint32_t row, const uint32_t *d, const int64_t *st,
+                                            const int64_t *ost, int r, int p0, int64_t &ib,
+                                            int64_t &ob) {
   for (int l = 1; l < r; l++) {
     if (l == p0) continue;
-    const int64_t c = x % d[l];
-    x /= d[l];
-    in_base += c * st[l];
-    out_base += c * ost[l];
+    const uint32_t c = row % d[l];
+    row /= d[l];
+    ib += c * st[l];
+    ob += c * ost[l];
   }
-  // read along input leg 0, write along output leg 0 (= input leg p0)
-  for (int q = ty; q < TT; q += 8) {
-    const int64_t ii = i0 + tx, jj = j0 + q;
-    if (ii < d[0] && jj < d[p0]) tile[q][tx] = src[in_base + ii * st[0] + jj * st[p0]];
-  }
-  __syncthreads();
-  for (int q = ty; q < TT; q += 8) {
-    const int64_t jj = j0 + tx, ii = i0 + q;
-    if (ii < d[0] && jj < d[p0]) dst[out_base + jj * ost[p0] + ii * ost[0]] = tile[tx][q];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) transpose_kernel(TransposeJob job, int64_t n_tiles) {
+  __shared__ T buf[PLANE_MAX];
+  __shared__ int64_t base_in[PLANES_MAX], base_out[PLANES_MAX];
+  const int r = job.rank;
+  const int p0 = job.perm[0];
+  const T *src = (const T *)job.in.data;
+  T *dst = (T *)job.out;
+  const int tid = threadIdx.x;
+  for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const int64_t b = job.tile_block[t];
+    const uint32_t local = (uint32_t)(t - job.tile_start[b]);
+    const int64_t *bb = job.in.begin + b * r, *be = job.in.end + b * r;
+    const int64_t *st = job.in.strides + b * r;
+    uint32_t d[TQ_MAXR];
+    for (int l = 0; l < r; l++) d[l] = (uint32_t)(be[l] - bb[l] + 1);
+    int64_t ost[TQ_MAXR];  // stride in the output of INPUT leg l
+    {
+      int64_t sacc = 1;
+      for (int q = 0; q < r; q++) {
+        ost[job.perm[q]] = sacc;
+        sacc *= d[job.perm[q]];
+      }
+    }
+    const PlanePlan pp = plane_plan(d, r, p0);
+    const int64_t ib0 = job.in.offsets[b], ob0 = job.out_off[b];
+    __syncthreads();  // the previous tile is done with the shared arrays
+    if (pp.mode == 2) {
+      // one 32 x 32 tile of a large plane
+      const uint32_t n0 = (d[0] + TT - 1) / TT, np = (d[p0] + TT - 1) / TT;
+      const uint32_t i0 = (local % n0) * TT, j0 = ((local / n0) % np) * TT;
+      int64_t ib = ib0, ob = ob0;
+      plane_bases(local / n0 / np, d, st, ost, r, p0, ib, ob);
+      T(*tile)[TT + 1] = reinterpret_cast<T(*)[TT + 1]>(buf);
+      const int tx = tid & 31, ty = tid >> 5;
+      for (int q = ty; q < TT; q += 8) {
+        const uint32_t ii = i0 + tx, jj = j0 + q;
+        if (ii < d[0] && jj < d[p0]) tile[q][tx] = src[ib + ii * st[0] + jj * st[p0]];
+      }
+      __syncthreads();
+      for (int q = ty; q < TT; q += 8) {
+        const uint32_t jj = j0 + tx, ii = i0 + q;
+        if (ii < d[0] && jj < d[p0]) dst[ob + jj * ost[p0] + ii * ost[0]] = tile[tx][q];
+      }
+      continue;
+    }
+    if (pp.mode == 0 && d[0] > (uint32_t)PLANE_MAX) {
+      // one PLANE_MAX-long piece of a long run
+      const uint32_t npc = (d[0] + PLANE_MAX - 1) / PLANE_MAX;
+      const uint32_t i0 = (local % npc) * PLANE_MAX;
+      int64_t ib = ib0, ob = ob0;
+      plane_bases(local / npc, d, st, ost, r, p0, ib, ob);
+      for (uint32_t i = i0 + tid; i < d[0] && i < i0 + PLANE_MAX; i += 256)
+        dst[ob + i * ost[0]] = src[ib + i * st[0]];
+      continue;
+    }
+    // batched planes: bases first, one thread per plane
+    const uint32_t row0 = local * pp.ppc;
+    const uint32_t nrows = pp.rows - row0 < pp.ppc ? pp.rows - row0 : pp.ppc;
+    if ((uint32_t)tid < nrows) {
+      int64_t ib = ib0, ob = ob0;
+      plane_bases(row0 + tid, d, st, ost, r, p0, ib, ob);
+      base_in[tid] = ib;
+      base_out[tid] = ob;
+    }
+    __syncthreads();
+    if (pp.mode == 0) {
+      const uint32_t n = nrows * d[0];
+      for (uint32_t e = tid; e < n; e += 256) {
+        const uint32_t pi = e / d[0], i = e - pi * d[0];
+        dst[base_out[pi] + i * ost[0]] = src[base_in[pi] + i * st[0]];
+      }
+      continue;
+    }
+    // mode 1: plane pi sits at buf[pi * P + i + j * (d0 + 1)]
+    const uint32_t d0 = d[0], dp = d[p0], PL = d0 * dp, n = nrows * PL;
+    for (uint32_t e = tid; e < n; e += 256) {
+      const uint32_t pi = e / PL, w = e - pi * PL, j = w / d0, i = w - j * d0;
+      buf[pi * pp.P + i + j * (d0 + 1)] = src[base_in[pi] + i * st[0] + j * st[p0]];
+    }
+    __syncthreads();
+    for (uint32_t f = tid; f < n; f += 256) {
+      const uint32_t pi = f / PL, w = f - pi * PL, i = w / dp, j = w - i * dp;
+      dst[base_out[pi] + j * ost[p0] + i * ost[0]] = buf[pi * pp.P + i + j * (d0 + 1)];
+    }
   }
 }
 
@@ -171,37 +240,51 @@ extern "C" tq_status tq_bs_hard_transpose(const tq_bs *t, const int64_t *perm, t
   TQ_CHECK(alloc_data(o, off, s));
   TQ_CHECK(sync_device_meta(o, s));
   if (t->nb) {
-    DevArray<int64_t> tiles, tile_start, total;
-    DevArray<int32_t> tile_block;
-    TQ_CHECK(tiles.alloc(t->nb, s));
-    TQ_CHECK(tile_start.alloc(t->nb, s));
-    TQ_CHECK(total.alloc(1, s));
-    const DevBS v = t->view();
-    count_launch(), transpose_tiles_kernel<<<(unsigned)((t->nb + 255) / 256), 256, 0, s>>>(v, (int32_t)perm[0],
-                                                                         tiles.p);
-    TQ_CHECK(scan_exclusive(tiles.p, tile_start.p, t->nb, total.p, s));
+    // tiles per block from the host metadata (no device round trip)
+    const int32_t p0 = (int32_t)perm[0];
+    std::vector<int64_t> h_start(t->nb);
     int64_t n_tiles = 0;
-    TQ_CUDA(cudaMemcpyAsync(&n_tiles, total.p, 8, cudaMemcpyDeviceToHost, s));
-    TQ_CUDA(cudaStreamSynchronize(s));
+    for (int64_t b = 0; b < t->nb; b++) {
+      uint32_t d[TQ_MAXR];
+      uint64_t prod = 1;
+      for (int32_t l = 0; l < r; l++) {
+        const int64_t x = t->h_end[b * r + l] - t->h_begin[b * r + l] + 1;
+        prod *= (uint64_t)x;
+        if (x >= (int64_t(1) << 31) || prod >= (uint64_t(1) << 31))
+          return fail(TQ_ERR_UNSUPPORTED, "a block of 2^31 elements or more");
+        d[l] = (uint32_t)x;
+      }
+      h_start[b] = n_tiles;
+      n_tiles += plane_plan(d, r, p0).tiles;
+    }
+    if (n_tiles > 0x7fffffffLL) return fail(TQ_ERR_UNSUPPORTED, "more than 2^31 transpose tiles");
+    if (t->nb > 0x7fffffffLL) return fail(TQ_ERR_UNSUPPORTED, "more than 2^31 blocks");
+    DevArray<int64_t> tile_start;
+    DevArray<int32_t> tile_block;
+    TQ_CHECK(tile_start.alloc(t->nb, s));
+    TQ_CHECK(tile_block.alloc(std::max<int64_t>(n_tiles, 1), s));
+    TQ_CUDA(cudaMemcpyAsync(tile_start.p, h_start.data(), t->nb * 8, cudaMemcpyHostToDevice, s));
+    TQ_CUDA(cudaStreamSynchronize(s));  // h_start dies with this function
     TransposeJob job;
-    job.in = v;
+    job.in = t->view();
     job.rank = r;
     for (int32_t l = 0; l < r; l++) job.perm[l] = (int32_t)perm[l];
     job.out_off = o->d_meta.p + 3 * o->nb * r;
     job.tile_start = tile_start.p;
+    job.tile_block = tile_block.p;
     job.nb = t->nb;
     job.out = o->data;
-    if (n_tiles > 0x7fffffffLL) return fail(TQ_ERR_UNSUPPORTED, "more than 2^31 transpose tiles");
-    if (t->nb > 0x7fffffffLL) return fail(TQ_ERR_UNSUPPORTED, "more than 2^31 blocks");
-    TQ_CHECK(tile_block.alloc(std::max<int64_t>(n_tiles, 1), s));
-    job.tile_block = tile_block.p;
     if (n_tiles) {
       count_launch(), tile_block_kernel<<<(unsigned)t->nb, 256, 0, s>>>(tile_start.p, t->nb, n_tiles,
                                                                          tile_block.p);
+      int dev = 0, sms = 0;
+      TQ_CUDA(cudaGetDevice(&dev));
+      TQ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+      const unsigned grid = (unsigned)std::min<int64_t>(n_tiles, 6 * (int64_t)sms);
       if (t->dtype == TQ_F64)
-        count_launch(), transpose_kernel<double><<<(unsigned)n_tiles, 256, 0, s>>>(job);
+        count_launch(), transpose_kernel<double><<<grid, 256, 0, s>>>(job, n_tiles);
       else
-        count_launch(), transpose_kernel<float><<<(unsigned)n_tiles, 256, 0, s>>>(job);
+        count_launch(), transpose_kernel<float><<<grid, 256, 0, s>>>(job, n_tiles);
       TQ_CUDA(cudaGetLastError());
     }
   }
