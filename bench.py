@@ -600,7 +600,7 @@ def peps_norm(tq):
 def cost_model(tq, n_live=24):
     """The learned cost model: trained on the GPU (library kernels) on the
     exhaustive tuner's measurements of 1,800 random contractions (seed 4),
-    judged on the 200 held-out ones: regret against exhaustive tuning and gain
+    evaluated on the 200 held-out ones: regret against exhaustive tuning and gain
     over the default schedule, from the stored measurements; then live runs of
     the model's proposal at 1e-10 on n_live held-out contractions."""
     import torch

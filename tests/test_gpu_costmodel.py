@@ -105,7 +105,7 @@ def test_plan_features(tq):
 
 def test_trained_model_regret_and_gain(tq):
     """Trained on the tuner's measurements of 1,800 random contractions (library
-    kernels only), judged on the 200 held out: the model's proposals stay close
+    kernels only), evaluated on the 200 held out: the model's proposals stay close
     to the exhaustive tuner (mean regret = mean of ms_pick / ms_best - 1) and
     beat the schedule the library takes without the model (5 slices for 1e-10,
     4 for 1e-8, tile width 96, no grouping) by a wide margin."""

@@ -14,8 +14,8 @@ score.  Training target of candidate c for a target accuracy eps:
     PENALTY                     otherwise
 where ms_best(eps) is the fastest candidate meeting eps, so a score is the
 predicted slowdown against the exhaustive choice, in octaves.  The tuner stays
-the fallback (a proposal that fails to run is replaced by its choice) and the
-judge (regret is measured against it).
+the fallback (a proposal that misses the target is replaced by its choice) and
+the yardstick (regret is measured against it).
 
 Device memory for the training arrays comes from torch (plumbing only: every
 forward, backward and update is a library kernel).
