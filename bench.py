@@ -417,6 +417,7 @@ def run_ours(args):
             bh.copy_(b)
             del A, B, a, b
             torch.cuda.empty_cache()
+            _lib.check(lib.tq_release_cached_memory())  # a fresh pool for the e2e passes
             line["e2e"] = e2e(tq, c, ah, bh, kw, 3)
         print(json.dumps(line))
     if world > 1:
