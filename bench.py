@@ -105,6 +105,24 @@ class Clocks:
                 "samples": len(rows)}
 
 
+# ---------------------------------------------------------------- replicas
+def max_over_ranks(ms, world, device):
+    """The slowest replica's time (every rank gets it): the job's step time."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_tflops(world, flops_per_replica, ms):
+    """Useful TFLOP/s of the whole job: every replica contracts the full
+    workload (weak scaling), all of them within the slowest one's time."""
+    return world * flops_per_replica / (ms / 1e3) / 1e12
+
+
 # ---------------------------------------------------------------- workload
 def structure(peak):
     from torque_gb300 import workloads
@@ -344,11 +362,8 @@ def run_ours(args):
     launches = lib.tq_debug_kernel_launches() - l0
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    value = world * flops / (ms / 1e3) / 1e12
+    ms = max_over_ranks(ms, world, "cuda")
+    value = whole_job_tflops(world, flops, ms)
 
     line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
