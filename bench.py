@@ -414,18 +414,12 @@ def run_ours(args):
             line["plain_fp64"] = fp64_subset(tq, c, A, a, b, kw)
         if not args.no_hbm:
             line["hbm_kernels"] = hbm_kernels(tq, c, A, B)
-        if not args.no_sweep:
-            line["batched_sweep"] = sweep(tq)
-        if not args.no_peps:
-            line["peps_norm"] = peps_norm(tq)
-        if not args.no_costmodel:
-            line["cost_model"] = cost_model(tq)
-
         line["cpu_baseline"] = dict(zip(("value", "cores", "sample"),
                                         cpu_sample(c, a, b, args.cpu_seconds)))
         line["cpu_baseline"].update({"unit": "TFLOP/s", "kind": "port"})
 
         if not args.no_e2e:
+            # right after the device-resident steps, in the same GPU state
             ah = torch.empty(a.numel(), dtype=torch.float64, pin_memory=True)
             bh = torch.empty(b.numel(), dtype=torch.float64, pin_memory=True)
             ah.copy_(a)
@@ -434,6 +428,15 @@ def run_ours(args):
             torch.cuda.empty_cache()
             _lib.check(lib.tq_release_cached_memory())  # a fresh pool for the e2e passes
             line["e2e"] = e2e(tq, c, ah, bh, kw, 3)
+            del ah, bh
+        _lib.check(lib.tq_release_cached_memory())
+
+        if not args.no_sweep:
+            line["batched_sweep"] = sweep(tq)
+        if not args.no_peps:
+            line["peps_norm"] = peps_norm(tq)
+        if not args.no_costmodel:
+            line["cost_model"] = cost_model(tq)
         print(json.dumps(line))
     if world > 1:
         dist.barrier()
@@ -670,27 +673,34 @@ def e2e(tq, c, ah, bh, kw, steps):
     from torque_gb300 import _lib
     an, bn = ah.numpy(), bh.numpy()
     ch = None
-    times = []
+    times, phases = [], []
     for s in range(steps + 1):
         torch.cuda.synchronize()
         t = time.perf_counter()
         A = tq.BlockSparseTensor(c.A.dimension, an, c.A.begin.T, c.A.end.T)
         B = tq.BlockSparseTensor(c.B.dimension, bn, c.B.begin.T, c.B.end.T)
+        t1 = time.perf_counter()  # creation from host memory returns after its copy
         P = tq.ContractionPlan(A, B, c.pairs, **kw)
         P.execute()
         P.check()
         C = P.result
         if ch is None:
             ch = torch.empty(C.n_elem, dtype=torch.float64, pin_memory=True)
+        t2 = time.perf_counter()
         _lib.check(_lib.load().tq_bs_copy_data(C.handle, ctypes.c_void_p(ch.data_ptr()),
                                                _lib.TQ_MEM_HOST, None))
-        dt = time.perf_counter() - t
+        t3 = time.perf_counter()
+        dt = t3 - t
         fl = P.flops
         del P, C, A, B
         if s > 0:  # the first pass pins pages and warms the allocator
             times.append(dt)
+            phases.append((t1 - t, t2 - t1, t3 - t2))
     dt = statistics.median(times)
+    ph = phases[times.index(dt)] if dt in times else phases[0]
     return {"value": fl / dt / 1e12, "unit": "TFLOP/s", "ms_per_step": dt * 1e3,
+            "phases_ms": {"h2d_create": ph[0] * 1e3, "plan_execute": ph[1] * 1e3,
+                          "d2h": ph[2] * 1e3},
             "h2d_bytes_per_step": 8 * (ah.numel() + bh.numel()),
             "d2h_bytes_per_step": 8 * int(ch.numel()), "steps": steps,
             "path": "tq_bs_create(host) x2 + tq_plan_create/execute + tq_bs_copy_data(host)"}
