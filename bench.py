@@ -105,6 +105,36 @@ class Clocks:
                 "samples": len(rows)}
 
 
+# ---------------------------------------------------------------- host placement
+def bind_near_gpu(dev):
+    """Run this process on the CPU cores attached to the GPU (its PCI device's
+    local CPU list), so pinned host buffers are allocated next to it: on a
+    multi-socket host a buffer on the far socket more than halves host-device
+    copy bandwidth.  Returns the cores, or None where the topology is not
+    readable."""
+    import torch
+    try:
+        uuid = str(torch.cuda.get_device_properties(dev).uuid)
+        q = subprocess.run(["nvidia-smi", "--query-gpu=pci.bus_id", "--format=csv,noheader",
+                            "-i", uuid if uuid.startswith("GPU-") else "GPU-" + uuid],
+                           capture_output=True, text=True, timeout=30)
+        bus = q.stdout.strip().splitlines()[0].strip().lower()
+        dom, rest = bus.split(":", 1)
+        path = "/sys/bus/pci/devices/%s:%s/local_cpulist" % (dom[-4:], rest)
+        with open(path) as f:
+            spec = f.read().strip()
+        cpus = set()
+        for part in spec.split(","):
+            lo, _, hi = part.partition("-")
+            cpus.update(range(int(lo), int(hi or lo) + 1))
+        if cpus:
+            os.sched_setaffinity(0, cpus)
+            return sorted(cpus)
+    except Exception:
+        pass
+    return None
+
+
 # ---------------------------------------------------------------- replicas
 def max_over_ranks(ms, world, device):
     """The slowest replica's time (every rank gets it): the job's step time."""
@@ -303,6 +333,7 @@ def run_ours(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    near = bind_near_gpu(local)
     if world > 1:
         dist.init_process_group("nccl")
     lib = tq.load()
@@ -428,6 +459,8 @@ def run_ours(args):
             torch.cuda.empty_cache()
             _lib.check(lib.tq_release_cached_memory())  # a fresh pool for the e2e passes
             line["e2e"] = e2e(tq, c, ah, bh, kw, 3)
+            line["e2e"]["host_cores"] = ("%d cores local to the GPU" % len(near)) if near else \
+                "unbound"
             del ah, bh
         _lib.check(lib.tq_release_cached_memory())
 
