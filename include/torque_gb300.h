@@ -97,6 +97,18 @@ tq_status tq_bs_create(tq_dtype dtype, int32_t rank, const int64_t *dimension,
                        const void *data, tq_memkind kind, tq_stream stream,
                        tq_bs **out);
 
+/* The same block list with every element zero (the reference's
+ * DenseTensor(dimension) and SparseTensor(dimension) constructors,
+ * src/gpu/dense.cuh:68-84, src/gpu/sparse.cuh:95-103, start from zeros). */
+tq_status tq_bs_create_zeros(tq_dtype dtype, int32_t rank, const int64_t *dimension,
+                             int64_t n_blocks, const int64_t *begin_points,
+                             const int64_t *end_points, const int64_t *index_tables,
+                             tq_stream stream, tq_bs **out);
+
+/* Overwrite all block data (n_elem elements; one for a rank-0 tensor) from
+ * host or device memory: DenseTensor::initialize (src/gpu/dense.cuh:172-184). */
+tq_status tq_bs_set_data(tq_bs *t, const void *data, tq_memkind kind, tq_stream stream);
+
 /* Copy constructor (block_sparse.cuh:306-327): deep device copy. */
 tq_status tq_bs_clone(const tq_bs *t, tq_stream stream, tq_bs **out);
 

@@ -10,6 +10,7 @@ import pytest
 from conftest import ROOT
 
 SRC = os.path.join(ROOT, "tests", "cpp", "block_sparse_kat.cpp")
+SRC_DS = os.path.join(ROOT, "tests", "cpp", "dense_sparse_kat.cpp")
 
 
 def cuda_include():
@@ -24,13 +25,13 @@ def cuda_include():
     pytest.skip("CUDA headers not found")
 
 
-def build_kat(tmp_path):
+def build_kat(tmp_path, src=SRC):
     from torque_gb300 import build as tq_build
     lib = tq_build.build()
-    exe = str(tmp_path / "block_sparse_kat")
+    exe = str(tmp_path / os.path.splitext(os.path.basename(src))[0])
     libdir = os.path.dirname(lib)
     cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"),
-           "-I" + cuda_include(), "-o", exe, SRC, "-L" + libdir, "-ltorque_gb300",
+           "-I" + cuda_include(), "-o", exe, src, "-L" + libdir, "-ltorque_gb300",
            "-Wl,-rpath," + libdir]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -39,11 +40,20 @@ def build_kat(tmp_path):
 
 def test_cpp_header_compiles(tmp_path):
     build_kat(tmp_path)
+    build_kat(tmp_path, SRC_DS)
 
 
 @pytest.mark.gpu
 def test_cpp_known_answers(tq, tmp_path):
     exe = build_kat(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "OK" in r.stdout
+
+
+@pytest.mark.gpu
+def test_cpp_dense_sparse_known_answers(tq, tmp_path):
+    exe = build_kat(tmp_path, SRC_DS)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "OK" in r.stdout

@@ -39,8 +39,10 @@ def _stream(stream) -> Optional[int]:
 def _blocks(points, rank: int) -> np.ndarray:
     """rank x n_blocks (arma::umat layout) -> flat [b*rank + l]."""
     a = np.asarray(points, dtype=np.int64)
+    if rank == 0:
+        return np.zeros((0, 0), np.int64)
     if a.ndim == 1:
-        a = a.reshape(rank, -1) if rank else a.reshape(0, -1)
+        a = a.reshape(rank, -1)
     if a.shape[0] != rank:
         raise _lib.TorqueError(_lib.TQ_ERR_INVALID, "Rank does not match")
     return np.ascontiguousarray(a.T)

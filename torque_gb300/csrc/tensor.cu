@@ -275,6 +275,49 @@ tq_status tq_bs_create(tq_dtype dtype, int32_t rank, const int64_t *dimension, i
   return TQ_OK;
 }
 
+tq_status tq_bs_create_zeros(tq_dtype dtype, int32_t rank, const int64_t *dimension,
+                             int64_t n_blocks, const int64_t *begin_points,
+                             const int64_t *end_points, const int64_t *index_tables,
+                             tq_stream stream, tq_bs **out) {
+  if (!out) return fail(TQ_ERR_INVALID, "out is NULL");
+  if (n_blocks < 0) return fail(TQ_ERR_INVALID, "negative block count");
+  if (rank == 0) return tq_bs_create_empty(dtype, 0, nullptr, out);
+  if (n_blocks && (!begin_points || !end_points))
+    return fail(TQ_ERR_INVALID, "begin/end points are NULL");
+  if (rank < 0 || rank > TQ_MAXR) return fail(TQ_ERR_UNSUPPORTED, "rank outside 0..12");
+  TQ_CHECK(check_boxes(rank, dimension, n_blocks, begin_points, end_points));
+  tq_bs *t = new_tensor(dtype, rank, dimension);
+  int64_t added = 0;
+  append_meta(t, n_blocks, begin_points, end_points, index_tables, &added);
+  tq_status st = alloc_data(t, added, (cudaStream_t)stream);
+  if (st == TQ_OK && added) {
+    const cudaError_t e = cudaMemsetAsync(t->data, 0, (size_t)added * dtype_size(dtype),
+                                          (cudaStream_t)stream);
+    if (e != cudaSuccess) st = cuda_fail(e, "cudaMemsetAsync");
+  }
+  if (st == TQ_OK) st = sync_device_meta(t, (cudaStream_t)stream);
+  if (st != TQ_OK) {
+    tq_bs_destroy(t);
+    return st;
+  }
+  *out = t;
+  return TQ_OK;
+}
+
+tq_status tq_bs_set_data(tq_bs *t, const void *data, tq_memkind kind, tq_stream stream) {
+  if (!t) return fail(TQ_ERR_INVALID, "tensor is NULL");
+  if (!data) return fail(TQ_ERR_INVALID, "Source data not allocated!");
+  const int64_t n = t->rank == 0 ? 1 : t->n_elem;
+  if (n == 0) return TQ_OK;
+  cudaError_t e = cudaMemcpyAsync(t->data, data, (size_t)n * dtype_size(t->dtype),
+                                  kind == TQ_MEM_HOST ? cudaMemcpyHostToDevice
+                                                      : cudaMemcpyDeviceToDevice,
+                                  (cudaStream_t)stream);
+  if (e == cudaSuccess && kind == TQ_MEM_HOST) e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync");
+  return TQ_OK;
+}
+
 tq_status tq_bs_clone(const tq_bs *src, tq_stream stream, tq_bs **out) {
   if (!src || !out) return fail(TQ_ERR_INVALID, "NULL argument");
   cudaStream_t s = (cudaStream_t)stream;
