@@ -100,6 +100,15 @@ __device__ __forceinline__ void plane_bases(uint32_t row, const uint32_t *d, con
   }
 }
 
+// x / d for x < 8192 and 1 <= d <= 4096 by a multiply with m = 2^32 / d
+// rounded up (exact over that range: checked for every x and d), d = 1 apart.
+struct SmallDiv {
+  uint32_t d, m;
+  __device__ __forceinline__ explicit SmallDiv(uint32_t dd)
+      : d(dd), m(dd > 1 ? 0xFFFFFFFFu / dd + 1u : 0u) {}
+  __device__ __forceinline__ uint32_t div(uint32_t x) const { return d > 1 ? __umulhi(x, m) : x; }
+};
+
 template <typename T>
 __global__ void __launch_bounds__(256) transpose_kernel(TransposeJob job, int64_t n_tiles) {
   __shared__ T buf[PLANE_MAX];
@@ -167,22 +176,25 @@ __global__ void __launch_bounds__(256) transpose_kernel(TransposeJob job, int64_
     }
     __syncthreads();
     if (pp.mode == 0) {
+      // nrows * d0 <= PLANE_MAX here
+      const SmallDiv by_d0(d[0]);
       const uint32_t n = nrows * d[0];
       for (uint32_t e = tid; e < n; e += 256) {
-        const uint32_t pi = e / d[0], i = e - pi * d[0];
+        const uint32_t pi = by_d0.div(e), i = e - pi * d[0];
         dst[base_out[pi] + i * ost[0]] = src[base_in[pi] + i * st[0]];
       }
       continue;
     }
-    // mode 1: plane pi sits at buf[pi * P + i + j * (d0 + 1)]
+    // mode 1: plane pi sits at buf[pi * P + i + j * (d0 + 1)]; n <= PLANE_MAX
     const uint32_t d0 = d[0], dp = d[p0], PL = d0 * dp, n = nrows * PL;
+    const SmallDiv by_pl(PL), by_d0(d0), by_dp(dp);
     for (uint32_t e = tid; e < n; e += 256) {
-      const uint32_t pi = e / PL, w = e - pi * PL, j = w / d0, i = w - j * d0;
+      const uint32_t pi = by_pl.div(e), w = e - pi * PL, j = by_d0.div(w), i = w - j * d0;
       buf[pi * pp.P + i + j * (d0 + 1)] = src[base_in[pi] + i * st[0] + j * st[p0]];
     }
     __syncthreads();
     for (uint32_t f = tid; f < n; f += 256) {
-      const uint32_t pi = f / PL, w = f - pi * PL, i = w / dp, j = w - i * dp;
+      const uint32_t pi = by_pl.div(f), w = f - pi * PL, i = by_dp.div(w), j = w - i * dp;
       dst[base_out[pi] + j * ost[p0] + i * ost[0]] = buf[pi * pp.P + i + j * (d0 + 1)];
     }
   }
