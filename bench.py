@@ -562,12 +562,13 @@ def fp64_subset(tq, c, A, a, b, kw):
                       "one full contraction each" % (sel.size, c.B.n_blocks, fl)}
 
 
-def sweep(tq, n=256, precision="ozaki", slices=5, replays=20):
+def sweep(tq, n=256, forms=(("ozaki", 5), ("bf16x3", 3)), replays=20):
     """PEPS-sweep site updates (E1 x T over (l,u), then X x E2 over (chi',r,d);
     D ~ U{4..10}, chi ~ U{16..64}, seed 3): n sequential plain-FP64 contract
     calls (symbolic + numeric each, as the reference runs them) against the same
     contractions planned once and run as one replayed CUDA graph of the batched
-    sliced form (one persistent GEMM launch per wave)."""
+    sliced form (one persistent GEMM launch per wave), for the FP64-level
+    (Ozaki) and the FP32-level (3 x bf16) forms."""
     import torch
     from torque_gb300 import workloads
     inst = workloads.peps_sweep(n, seed=3)
@@ -590,36 +591,40 @@ def sweep(tq, n=256, precision="ozaki", slices=5, replays=20):
     t = time.perf_counter()
     ref = sequential()
     t_seq = time.perf_counter() - t
-    # plans: the symbolic stage once
-    t = time.perf_counter()
-    p1 = [tq.ContractionPlan(E1, T, s.pairs1, precision=precision, slices=slices, layout="reduced")
-          for s, (T, E1, E2) in zip(inst, ts)]
-    p2 = [tq.ContractionPlan(a.result, E2, s.pairs2, precision=precision, slices=slices,
-                             layout="reduced") for a, s, (T, E1, E2) in zip(p1, inst, ts)]
-    torch.cuda.synchronize()
-    t_plan = time.perf_counter() - t
-    flops = sum(p.flops for p in p1 + p2)
-    batch = tq.Batch(p1 + p2, waves=[0] * n + [1] * n)
-    batch.graph_launch()
-    batch.check()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record()
-    for _ in range(replays):
+    res = {"instances": n, "sequential_fp64_ms": t_seq * 1e3}
+    for precision, slices in forms:
+        # plans: the symbolic stage once
+        t = time.perf_counter()
+        p1 = [tq.ContractionPlan(E1, T, s.pairs1, precision=precision, slices=slices,
+                                 layout="reduced") for s, (T, E1, E2) in zip(inst, ts)]
+        p2 = [tq.ContractionPlan(a.result, E2, s.pairs2, precision=precision, slices=slices,
+                                 layout="reduced") for a, s, (T, E1, E2) in zip(p1, inst, ts)]
+        torch.cuda.synchronize()
+        t_plan = time.perf_counter() - t
+        flops = sum(p.flops for p in p1 + p2)
+        batch = tq.Batch(p1 + p2, waves=[0] * n + [1] * n)
         batch.graph_launch()
-    ev1.record()
-    torch.cuda.synchronize()
-    batch.check()
-    t_graph = ev0.elapsed_time(ev1) / 1e3 / replays
-    err = 0.0
-    for a, b in zip(p2, ref):
-        x, y = a.result.data(), b.data()
-        err = max(err, float(np.max(np.abs(x - y)) / np.max(np.abs(y))))
-    return {"instances": n, "useful_flop": flops,
-            "sequential_fp64_tflops": flops / t_seq / 1e12, "sequential_fp64_ms": t_seq * 1e3,
-            "graph_tflops": flops / t_graph / 1e12, "graph_ms": t_graph * 1e3,
-            "speedup": t_seq / t_graph, "plan_ms_once": t_plan * 1e3,
-            "graph_kernels": batch.kernels, "precision": precision, "slices": slices,
-            "max_rel_err_vs_fp64": err}
+        batch.check()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(replays):
+            batch.graph_launch()
+        ev1.record()
+        torch.cuda.synchronize()
+        batch.check()
+        t_graph = ev0.elapsed_time(ev1) / 1e3 / replays
+        err = 0.0
+        for a, b in zip(p2, ref):
+            x, y = a.result.data(), b.data()
+            err = max(err, float(np.max(np.abs(x - y)) / np.max(np.abs(y))))
+        res["useful_flop"] = flops
+        res["sequential_fp64_tflops"] = flops / t_seq / 1e12
+        res[precision] = {"slices": slices, "graph_ms": t_graph * 1e3,
+                          "graph_tflops": flops / t_graph / 1e12, "speedup": t_seq / t_graph,
+                          "plan_ms_once": t_plan * 1e3, "graph_kernels": batch.kernels,
+                          "max_rel_err_vs_fp64": err}
+        del batch, p1, p2
+    return res
 
 
 def peps_norm(tq):
