@@ -360,6 +360,8 @@ def run_ours(args):
                 "tuning_s": time.perf_counter() - t}
         kw.update(tile_n=cands[best]["tile_n"], native_fill=cands[best]["native_fill"])
         del P0
+        torch.cuda.synchronize()
+        _lib.check(lib.tq_release_cached_memory())  # the candidates' scratch back to the driver
 
     def step(profile=False):
         P = tq.ContractionPlan(A, B, c.pairs, **kw)
