@@ -46,6 +46,9 @@ def parse():
     p.add_argument("--precision", default="ozaki", choices=["ozaki", "bf16x3", "native"])
     p.add_argument("--slices", type=int, default=5)
     p.add_argument("--peak", type=float, default=48.0, help="sector size peak (48: full size)")
+    p.add_argument("--qmax", type=int, default=16,
+                   help="charges -qmax..qmax per leg (16: full size; smaller keeps only the "
+                        "central, largest sectors)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
@@ -154,9 +157,9 @@ def whole_job_tflops(world, flops_per_replica, ms):
 
 
 # ---------------------------------------------------------------- workload
-def structure(peak):
+def structure(peak, qmax=16):
     from torque_gb300 import workloads
-    return workloads.uneven_u1(peak=peak, data=False)
+    return workloads.uneven_u1(peak=peak, qmax=qmax, data=False)
 
 
 def block_offsets(bl):
@@ -287,7 +290,7 @@ def run_reference(args):
     if rank != 0:
         return
     import torch
-    c = structure(args.peak)
+    c = structure(args.peak, args.qmax)
     # inputs are generated on the device (same generator as our arm) and the
     # sampled blocks copied to the host
     torch.cuda.set_device(0)
@@ -314,9 +317,9 @@ def run_reference(args):
 
 
 def config_dict(args, c):
-    return {"workload": "u1-rank4 A[a,b,c,d]xB[c,d,e,f] over (c,d), 33 sectors "
+    return {"workload": "u1-rank4 A[a,b,c,d]xB[c,d,e,f] over (c,d), %d sectors "
                         "s_q=max(1,round(%g*exp(-q^2/32))), %d per leg, %d blocks/tensor" %
-                        (args.peak, int(c.A.dimension[0]), c.A.n_blocks),
+                        (2 * args.qmax + 1, args.peak, int(c.A.dimension[0]), c.A.n_blocks),
             "pairs": None, "layout": "reduced", "precision": args.precision,
             "slices": args.slices if args.precision != "native" else None,
             "l2": "inputs (2 x %.1f GB) exceed L2; no flush" % (8 * c.A.n_elem / 1e9),
@@ -337,7 +340,7 @@ def run_ours(args):
     if world > 1:
         dist.init_process_group("nccl")
     lib = tq.load()
-    c = structure(args.peak)
+    c = structure(args.peak, args.qmax)
     g = torch.Generator(device="cuda")
     g.manual_seed(2)
     a = torch.randn(c.A.n_elem, dtype=torch.float64, device="cuda", generator=g)

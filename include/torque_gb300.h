@@ -5,7 +5,7 @@
  * (torque::gpu::BlockSparseTensor<T>, src/gpu/block_sparse.cuh).  The C++
  * header include/torque_gb300/block_sparse.hpp rebuilds the reference class on
  * top of these entry points; other languages bind them directly (ctypes, cgo,
- * JNI: see INTEGRATION.md).
+ * JNI) through the plain pointers, sizes and status codes below.
  *
  * Conventions kept from the reference:
  *   - column-major: leg 0 is fastest (src/util/space.h:11-24);
@@ -158,6 +158,23 @@ tq_status tq_bs_contract(const tq_bs *A, const tq_bs *B, int32_t n_legs,
                          const int64_t *a_legs, const int64_t *b_legs,
                          const tq_contract_opts *opts, tq_stream stream, tq_bs **out);
 
+/* The block list contract would produce, from its symbolic stage alone: the
+ * pair matching of block_in_range (src/tensor/block_sparse.cpp:6-175) and the
+ * group assembly of contract (block_sparse.cuh:620-674), with no block
+ * GEMM run and no result data allocated, so the structure of a result too large
+ * to hold can still be read.  layout is a tq_layout.  *n_blocks and *n_elem
+ * receive the result's block and element counts; when cap >= *n_blocks the
+ * non-NULL host arrays are filled: begin_points and end_points (rank x
+ * n_blocks, as tq_bs_metadata), block_offsets (n_blocks) and, in the reference
+ * layout only, pair_a / pair_b (n_blocks: the A and B block of each output
+ * block).  Call once with cap = 0 to size the arrays. */
+tq_status tq_contract_blocks(const tq_bs *A, const tq_bs *B, int32_t n_legs,
+                             const int64_t *a_legs, const int64_t *b_legs, int32_t layout,
+                             int64_t cap, int64_t *n_blocks, int64_t *n_elem,
+                             int64_t *begin_points, int64_t *end_points,
+                             int64_t *block_offsets, int64_t *pair_a, int64_t *pair_b,
+                             tq_stream stream);
+
 /* hard_transpose (block_sparse.cuh:1031-1122): permute the legs of every block;
  * new leg l is old leg perm[l]. */
 tq_status tq_bs_hard_transpose(const tq_bs *t, const int64_t *perm, tq_stream stream,
@@ -295,7 +312,9 @@ typedef struct tq_batch tq_batch;
  * orders dependent contractions: a wave may read results of earlier waves
  * (e.g. the two contractions of a PEPS site update).  Native-precision and
  * rank-0 plans run after the tensor-core launch of their wave.  The plans must
- * outlive the batch. */
+ * outlive the batch.  Rescheduling a plan (tq_plan_reschedule, tq_autotune)
+ * frees the arrays the batch's device tables point into: every batch built
+ * from it before then refuses to run (TQ_ERR_INVALID) and must be built again. */
 tq_status tq_batch_create(tq_plan *const *plans, int32_t n, const int32_t *wave,
                           tq_stream stream, tq_batch **out);
 /* The numeric stage of every plan, ordered on stream; no host synchronisation,

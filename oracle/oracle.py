@@ -195,6 +195,24 @@ def contract(A: HostBS, B: HostBS, pairs, mode: int = 0):
     return ob[:npairs, :ro], oe[:npairs, :ro], off[:npairs], data[:size]
 
 
+def contract_blocks(A: HostBS, B: HostBS, pairs):
+    """The reference layout's block list without its values: pair list (A
+    block, B block), output begin/end and offsets (orc_match + the box and
+    offset loop of orc_contract with no data), for results too large to hold."""
+    al, bl, nc = _legs(pairs)
+    pa, pb = match(A, B, pairs)
+    ca, cb = A.c(), B.c()
+    ro = A.rank + B.rank - 2 * nc
+    n = pa.size
+    ob = np.zeros((max(n, 1), max(ro, 1)), np.int64)
+    oe = np.zeros_like(ob)
+    off = np.zeros(max(n, 1), np.int64)
+    st = lib().orc_contract(ctypes.byref(ca), ctypes.byref(cb), nc, _p64(al), _p64(bl), 0,
+                            _p64(ob), _p64(oe), _p64(off), None)
+    assert st == 0
+    return pa, pb, ob[:n, :ro], oe[:n, :ro], off[:n]
+
+
 def pair_values(A: HostBS, B: HostBS, pairs, i: int, j: int, mode: int = 0, j_block: int = 0):
     al, bl, nc = _legs(pairs)
     ca, cb = A.c(), B.c()

@@ -78,3 +78,48 @@ def test_batch_matches_sequential_and_fp64(tq, precision, slices, tol):
     dim, b, e, t, o = R.metadata()
     got = orc.densify(orc.HostBS(dim, b.T, e.T, R.data(), t.T))
     assert np.max(np.abs(got - Y)) <= 1e-12 * np.max(np.abs(Y))
+
+
+def test_rescheduled_plan_invalidates_batch(tq):
+    """A batch's device tables point into its plans' schedule arrays; once a
+    plan is rescheduled the batch refuses to run (plain execute and graph
+    replay) instead of reading freed memory, and a batch built again runs."""
+    inst = workloads.peps_sweep(4, seed=32)
+    keep, p1, p2 = make_plans(tq, inst, "ozaki", 5)
+    batch = tq.Batch(p1 + p2, waves=[0] * len(p1) + [1] * len(p2))
+    batch.graph_launch()
+    batch.check()
+    want = results(p2)
+    p1[1].reschedule("ozaki", slices=5, tile_n=64)
+    for call in (batch.execute, batch.graph_launch):
+        with pytest.raises(tq.TorqueError) as ei:
+            call()
+        assert ei.value.status == 1 and "rescheduled" in str(ei.value)
+    again = tq.Batch(p1 + p2, waves=[0] * len(p1) + [1] * len(p2))
+    again.graph_launch()
+    again.check()
+    for x, y in zip(want, results(p2)):
+        assert np.max(np.abs(x - y)) <= 1e-10 * np.max(np.abs(y))
+
+
+@pytest.mark.parametrize("precision,slices,tol", [("ozaki", 5, 1e-10), ("bf16x3", 3, 1e-5)])
+def test_full_sweep_256_instances_against_fp64(tq, precision, slices, tol):
+    """The whole batched PEPS sweep of the benchmark (256 site updates, seed 3)
+    as one replayed graph, every instance's result against the plain FP64 form
+    of the same contractions (elementwise, scaled by the instance's max |C|)."""
+    inst = workloads.peps_sweep(256, seed=3)
+    keep, p1, p2 = make_plans(tq, inst, precision, slices)
+    batch = tq.Batch(p1 + p2, waves=[0] * len(p1) + [1] * len(p2))
+    batch.graph_launch()
+    batch.check()
+    got = results(p2)
+    del batch, p1, p2, keep
+    keep64, q1, q2 = make_plans(tq, inst, "native")
+    worst = 0.0
+    for q, (a, b) in enumerate(zip(q1, q2)):
+        a.execute()
+        b.execute()
+        y = b.result.data()
+        worst = max(worst, float(np.max(np.abs(got[q] - y)) / np.max(np.abs(y))))
+    print("256-instance sweep, %s: max rel err vs FP64 %.3e" % (precision, worst))
+    assert worst <= tol

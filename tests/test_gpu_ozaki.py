@@ -81,8 +81,9 @@ def test_extreme_scales_and_zero_rows(tq, scale):
 
 
 def test_long_fused_k(tq):
-    """Output blocks whose fused K spans several 512-column exact flushes
-    (sectors up to 24 wide: k up to 576 per pair, tens of pairs per block),
+    """Output blocks whose fused K spans many 336-column exact accumulator
+    retirements (sectors up to 24 wide: k up to 576 per pair, tens of pairs per
+    block),
     sampled blocks checked against the oracle."""
     u = workloads.uneven_u1(peak=24.0, seed=7)
     A, B, hA, hB = gpu_pair(tq, u)

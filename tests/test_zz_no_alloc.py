@@ -19,9 +19,10 @@ def test_noalloc_nest_sum_matches_allocating_entry_point(tq):
     lib = tq.load()
     g = torch.Generator(device="cuda")
     g.manual_seed(17)
-    # two multi-tile calls in a row (the second reuses the shared static scratch),
-    # then a single-tile one
-    for n in (3_000_001, 4_194_304, 1000):
+    # multi-tile calls in a row (each reuses the shared static scratch): two
+    # large ones, then smaller ones (2 and 3 tiles of 2048 counts) that must
+    # not read tile sums a larger earlier call left behind, then a single-tile one
+    for n in (3_000_001, 4_194_304, 2049, 4097, 1000):
         x = torch.randint(0, 100_000, (n,), dtype=torch.int64, device="cuda", generator=g)
         ref_o = torch.empty(n, dtype=torch.int64, device="cuda")
         ref_t = torch.empty(1, dtype=torch.int64, device="cuda")

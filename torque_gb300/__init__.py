@@ -6,9 +6,10 @@ helpers (charge-sector constructors, synthetic workloads, the PEPS-norm driver,
 the cost model's data and proposal logic).
 """
 from ._lib import TorqueError, load  # noqa: F401
-from .block_sparse import Batch, BlockSparseTensor, ContractionPlan  # noqa: F401
+from .block_sparse import Batch, BlockSparseTensor, ContractionPlan, contract_blocks  # noqa: F401
 from .dense import DenseTensor, SparseTensor  # noqa: F401
 from .sectors import BlockList, Leg, charge_blocks  # noqa: F401
 
-__all__ = ["BlockSparseTensor", "ContractionPlan", "Batch", "DenseTensor", "SparseTensor",
+__all__ = ["BlockSparseTensor", "ContractionPlan", "Batch", "contract_blocks", "DenseTensor",
+           "SparseTensor",
            "TorqueError", "Leg", "BlockList", "charge_blocks", "load"]

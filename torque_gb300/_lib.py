@@ -54,6 +54,8 @@ SIGNATURES = {
     "tq_bs_device_data": (ST, [P, PP]),
     "tq_bs_copy_data": (ST, [P, P, I32, P]),
     "tq_bs_contract": (ST, [P, P, I32, P64, P64, ctypes.POINTER(ContractOpts), P, PP]),
+    "tq_contract_blocks": (ST, [P, P, I32, P64, P64, I32, I64, P64, P64, P64, P64, P64, P64,
+                                P64, P]),
     "tq_bs_hard_transpose": (ST, [P, P64, P, PP]),
     "tq_bs_slice": (ST, [P, P64, P, PP]),
     "tq_bs_fuse_legs": (ST, [P, I32, I64, P64, I64, P64, P64, P, PP]),

@@ -75,6 +75,22 @@ class BlockSparseTensor:
                                   _stream(stream), ctypes.byref(self._h)))
         self._keep = None
 
+    @classmethod
+    def zeros(cls, dimension, begin_points, end_points, index_tables=None, dtype=np.float64,
+              stream=None) -> "BlockSparseTensor":
+        """The block list with every element zero (tq_bs_create_zeros)."""
+        dim = _i64(dimension)
+        rank = dim.size
+        b = _blocks(begin_points, rank)
+        e = _blocks(end_points, rank)
+        t = None if index_tables is None else _blocks(index_tables, rank)
+        h = ctypes.c_void_p()
+        check(load().tq_bs_create_zeros(_DT[np.dtype(dtype)], rank, _p64(dim),
+                                        b.shape[0] if rank else 0, _p64(b), _p64(e),
+                                        None if t is None else _p64(t), _stream(stream),
+                                        ctypes.byref(h)))
+        return cls(_handle=h)
+
     # ------------------------------------------------------------ helpers
     @staticmethod
     def _data_arg(src, dtype):
@@ -273,6 +289,41 @@ class BlockSparseTensor:
         h = ctypes.c_void_p()
         check(load().tq_bs_clone(self._h, _stream(stream), ctypes.byref(h)))
         return BlockSparseTensor(_handle=h)
+
+
+def contract_blocks(A: "BlockSparseTensor", B: "BlockSparseTensor", contracting_indices,
+                    layout="reference", stream=None):
+    """The block list A.contract(B, ...) would produce, from the symbolic stage
+    alone (tq_contract_blocks: nothing computed, no result data allocated).
+    Returns dict(begin, end, offsets: [n_blocks, rank] / [n_blocks] int64,
+    n_elem, and for the reference layout pair_a / pair_b: each output block's
+    A and B block)."""
+    ci = np.asarray(contracting_indices, dtype=np.int64).reshape(-1, 2)
+    al, bl = _i64(ci[:, 0]), _i64(ci[:, 1])
+    lay = _lib.LAYOUTS[layout]
+    nb, ne = ctypes.c_int64(), ctypes.c_int64()
+    lib = load()
+    check(lib.tq_contract_blocks(A._h, B._h, ci.shape[0], _p64(al), _p64(bl), lay, 0,
+                                 ctypes.byref(nb), ctypes.byref(ne), None, None, None, None,
+                                 None, _stream(stream)))
+    n = nb.value
+    rank = A.rank + B.rank - 2 * ci.shape[0]
+    begin = np.zeros((max(n, 1), max(rank, 1)), np.int64)
+    end = np.zeros_like(begin)
+    off = np.zeros(max(n, 1), np.int64)
+    ref = layout == "reference"
+    pa = np.zeros(max(n, 1), np.int64) if ref else None
+    pb = np.zeros(max(n, 1), np.int64) if ref else None
+    if n:
+        check(lib.tq_contract_blocks(A._h, B._h, ci.shape[0], _p64(al), _p64(bl), lay, n,
+                                     ctypes.byref(nb), ctypes.byref(ne), _p64(begin),
+                                     _p64(end), _p64(off), _p64(pa) if ref else None,
+                                     _p64(pb) if ref else None, _stream(stream)))
+    out = {"begin": begin[:n, :rank], "end": end[:n, :rank], "offsets": off[:n],
+           "n_elem": ne.value}
+    if ref:
+        out["pair_a"], out["pair_b"] = pa[:n], pb[:n]
+    return out
 
 
 def make_opts(precision="native", layout="reference", slices=0, tile_n=0, native_fill=0):

@@ -139,13 +139,12 @@ tq_status tq_plan_features(const tq_plan *plan, double target_rel_err, float *fe
   return plan_features(plan, target_rel_err, features, (cudaStream_t)stream);
 }
 
-tq_status tq_autotune(tq_plan *plan, double target_rel_err, tq_tune_entry *cands,
-                      int32_t n_cands, int32_t reps, int32_t *best, tq_stream stream) {
-  if (!plan || (n_cands > 0 && !cands) || !best) return fail(TQ_ERR_INVALID, "NULL argument");
-  if (n_cands < 0 || reps < 1) return fail(TQ_ERR_INVALID, "bad candidate or repetition count");
-  if (plan->A->dtype != TQ_F64) return fail(TQ_ERR_UNSUPPORTED, "the tuner takes float64 tensors");
-  cudaStream_t s = (cudaStream_t)stream;
-  const tq_contract_opts keep = plan->opts;
+}  // extern "C"
+
+namespace tq {
+static tq_status autotune_run(tq_plan *plan, const tq_contract_opts &keep, double target_rel_err,
+                              tq_tune_entry *cands, int32_t n_cands, int32_t reps, int32_t *best,
+                              cudaStream_t s) {
   EventPair ev;
   TQ_CUDA(cudaEventCreate(&ev.e[0]));
   TQ_CUDA(cudaEventCreate(&ev.e[1]));
@@ -204,6 +203,27 @@ tq_status tq_autotune(tq_plan *plan, double target_rel_err, tq_tune_entry *cands
   const tq_contract_opts fin = *best >= 0 ? cands[*best].opts : keep;
   TQ_CHECK(plan_reschedule(plan, fin, s));
   return TQ_OK;
+}
+}  // namespace tq
+
+extern "C" {
+
+tq_status tq_autotune(tq_plan *plan, double target_rel_err, tq_tune_entry *cands,
+                      int32_t n_cands, int32_t reps, int32_t *best, tq_stream stream) {
+  if (!plan || (n_cands > 0 && !cands) || !best) return fail(TQ_ERR_INVALID, "NULL argument");
+  if (n_cands < 0 || reps < 1) return fail(TQ_ERR_INVALID, "bad candidate or repetition count");
+  if (plan->A->dtype != TQ_F64) return fail(TQ_ERR_UNSUPPORTED, "the tuner takes float64 tensors");
+  cudaStream_t s = (cudaStream_t)stream;
+  const tq_contract_opts keep = plan->opts;
+  const tq_status st = autotune_run(plan, keep, target_rel_err, cands, n_cands, reps, best, s);
+  if (st != TQ_OK) {
+    // every failure leaves the plan on the caller's schedule (the first error's
+    // message is kept)
+    const std::string msg = tq_last_error_string();
+    *best = -1;
+    if (plan_reschedule(plan, keep, s) == TQ_OK) fail(st, msg);
+  }
+  return st;
 }
 
 }  // extern "C"

@@ -23,6 +23,7 @@ struct tq_batch {
   };
   std::vector<std::unique_ptr<Wave>> waves;
   std::vector<tq_plan *> plans;
+  std::vector<uint64_t> gens;  // each plan's schedule generation when the batch was built
   cudaStream_t capture_stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -33,6 +34,24 @@ struct tq_batch {
     if (capture_stream) cudaStreamDestroy(capture_stream);
   }
 };
+
+// The batch's device tables point into its plans' schedule arrays, which a
+// reschedule frees and rebuilds: such a batch must be built again.
+static tq_status batch_current(const tq_batch *b) {
+  for (size_t i = 0; i < b->plans.size(); i++)
+    if (b->plans[i]->sched_gen != b->gens[i])
+      return fail(TQ_ERR_INVALID,
+                  "plan " + std::to_string(i) +
+                      " was rescheduled after the batch was built; build the batch again");
+  return TQ_OK;
+}
+
+static void batch_drop_graph(tq_batch *b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+}
 
 static tq_status batch_run(tq_batch *b, cudaStream_t s) {
   for (auto &w : b->waves) {
@@ -61,6 +80,7 @@ tq_status tq_batch_create(tq_plan *const *plans, int32_t n, const int32_t *wave,
   cudaStream_t s = (cudaStream_t)stream;
   std::unique_ptr<tq_batch> b(new tq_batch());
   b->plans.assign(plans, plans + n);
+  for (int32_t k = 0; k < n; k++) b->gens.push_back(plans[k]->sched_gen);
   int32_t i = 0;
   while (i < n) {
     const int32_t wv = wave ? wave[i] : 0;
@@ -93,6 +113,7 @@ tq_status tq_batch_create(tq_plan *const *plans, int32_t n, const int32_t *wave,
 
 tq_status tq_batch_execute(tq_batch *b, tq_stream stream) {
   if (!b) return fail(TQ_ERR_INVALID, "batch is NULL");
+  TQ_CHECK(batch_current(b));
   const int64_t k0 = tq_debug_kernel_launches();
   TQ_CHECK(batch_run(b, (cudaStream_t)stream));
   b->kernels = tq_debug_kernel_launches() - k0;
@@ -101,22 +122,31 @@ tq_status tq_batch_execute(tq_batch *b, tq_stream stream) {
 
 tq_status tq_batch_graph_launch(tq_batch *b, tq_stream stream) {
   if (!b) return fail(TQ_ERR_INVALID, "batch is NULL");
+  TQ_CHECK(batch_current(b));
   if (!b->exec) {
-    // capture on a private stream (the legacy stream cannot be captured)
-    TQ_CUDA(cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking));
+    // capture on a private stream (the legacy stream cannot be captured), made
+    // once per batch; a failed capture or instantiation leaves no graph behind
+    if (!b->capture_stream)
+      TQ_CUDA(cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking));
+    batch_drop_graph(b);
     TQ_CUDA(cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal));
     const int64_t k0 = tq_debug_kernel_launches();
     tq_status st = batch_run(b, b->capture_stream);
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(b->capture_stream, &g);
-    if (st != TQ_OK) {
+    if (st != TQ_OK || e != cudaSuccess) {
       if (g) cudaGraphDestroy(g);
-      return st;
+      if (st != TQ_OK) return st;
+      TQ_CUDA(e);
     }
-    TQ_CUDA(e);
     b->graph = g;
     b->kernels = tq_debug_kernel_launches() - k0;
-    TQ_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    const cudaError_t ei = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (ei != cudaSuccess) {
+      b->exec = nullptr;
+      batch_drop_graph(b);
+      TQ_CUDA(ei);
+    }
   }
   TQ_CUDA(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
   return TQ_OK;

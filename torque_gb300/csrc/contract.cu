@@ -552,9 +552,12 @@ tq_status validate_legs(const tq_bs *A, const tq_bs *B, int32_t n_legs, const in
   return TQ_OK;
 }
 
+// structure_only: the symbolic stage alone (pairs, output boxes, offsets); the
+// result's data are not allocated and no work list is built, so the plan and
+// its result are for reading the block list only and never leave the library.
 tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,
                      const int64_t *b_legs, const tq_contract_opts *opts, cudaStream_t s,
-                     tq_plan **plan_out, tq_bs **out) {
+                     tq_plan **plan_out, tq_bs **out, bool structure_only = false) {
   LegSpec L;
   TQ_CHECK(validate_legs(A, B, n_legs, a_legs, b_legs, L));
   tq_contract_opts o = {TQ_PREC_NATIVE, TQ_LAYOUT_REFERENCE, 0, 0, 0, 0};
@@ -691,6 +694,16 @@ tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64
     TQ_CUDA(cudaStreamSynchronize(s));
     P->flops = 2.0 * (double)h[1];
     P->n_tiles = h[3];
+    if (structure_only) {
+      C->n_elem = h[2];
+      C->host_valid = false;
+      C->dev_valid = true;
+      P->C = C;
+      Cguard.release();
+      *out = C;
+      *plan_out = P.release();
+      return TQ_OK;
+    }
     TQ_CHECK(alloc_data(C, h[2], s));
     TQ_CHECK(native_work(P.get(), tiles.p, P->tile_start.p, P->n_tiles, P->nat, s));
     C->host_valid = false;
@@ -723,6 +736,7 @@ tq_status plan_reschedule(tq_plan *P, const tq_contract_opts &o, cudaStream_t s)
                 "tensor-core precision or the reduced layout to reschedule it");
   // wait for launches that still read the old schedule's arrays
   TQ_CUDA(cudaStreamSynchronize(s));
+  P->sched_gen++;
   P->opts = o;
   P->tc = o.precision != TQ_PREC_NATIVE;
   P->tc_tiles = P->hyb_tiles = 0;
@@ -816,6 +830,45 @@ tq_status tq_plan_last_timings(tq_plan *plan, float *prepare_ms, float *gemm_ms)
 tq_status tq_plan_check(tq_plan *plan, tq_stream stream) {
   if (!plan) return fail(TQ_ERR_INVALID, "plan is NULL");
   return plan_check(plan, (cudaStream_t)stream);
+}
+
+tq_status tq_contract_blocks(const tq_bs *A, const tq_bs *B, int32_t n_legs,
+                            const int64_t *a_legs, const int64_t *b_legs, int32_t layout,
+                            int64_t cap, int64_t *n_blocks, int64_t *n_elem,
+                            int64_t *begin_points, int64_t *end_points, int64_t *block_offsets,
+                            int64_t *pair_a, int64_t *pair_b, tq_stream stream) {
+  if (!A || !B || !n_blocks) return fail(TQ_ERR_INVALID, "NULL argument");
+  if (cap < 0) return fail(TQ_ERR_INVALID, "negative capacity");
+  if ((pair_a || pair_b) && layout != TQ_LAYOUT_REFERENCE)
+    return fail(TQ_ERR_INVALID, "block pairs are one per output block only in the reference layout");
+  cudaStream_t s = (cudaStream_t)stream;
+  tq_contract_opts o = {TQ_PREC_NATIVE, layout, 0, 0, 0, 0};
+  tq_plan *P = nullptr;
+  tq_bs *C = nullptr;
+  TQ_CHECK(plan_build(A, B, n_legs, a_legs, b_legs, &o, s, &P, &C, true));
+  std::unique_ptr<tq_plan, tq_status (*)(tq_plan *)> Pg(P, tq_plan_destroy);
+  std::unique_ptr<tq_bs, tq_status (*)(tq_bs *)> Cg(C, tq_bs_destroy);
+  const int64_t nb = C->rank == 0 ? 0 : C->nb;
+  *n_blocks = nb;
+  if (n_elem) *n_elem = C->rank == 0 ? 1 : C->n_elem;
+  if (cap < nb || nb == 0) return TQ_OK;
+  TQ_CHECK(sync_host_meta(C, s));
+  const size_t r = (size_t)C->rank;
+  if (begin_points) std::copy(C->h_begin.begin(), C->h_begin.begin() + nb * r, begin_points);
+  if (end_points) std::copy(C->h_end.begin(), C->h_end.begin() + nb * r, end_points);
+  if (block_offsets) std::copy(C->h_offsets.begin(), C->h_offsets.begin() + nb, block_offsets);
+  if (pair_a || pair_b) {
+    std::vector<int32_t> h((size_t)nb);
+    for (int side = 0; side < 2; side++) {
+      int64_t *dst = side ? pair_b : pair_a;
+      if (!dst) continue;
+      TQ_CUDA(cudaMemcpyAsync(h.data(), side ? P->pb.p : P->pa.p, (size_t)nb * 4,
+                              cudaMemcpyDeviceToHost, s));
+      TQ_CUDA(cudaStreamSynchronize(s));
+      for (int64_t q = 0; q < nb; q++) dst[q] = h[(size_t)q];
+    }
+  }
+  return TQ_OK;
 }
 
 tq_status tq_bs_contract(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,

@@ -47,6 +47,9 @@ struct tq_plan {
   int64_t KA = 0, KB = 0;  // free-box key ranges (tensor-core plans, reduced layout)
   bool keys = false;       // keyA/keyB were made
   bool sched_ok = true;    // false after a failed reschedule: execute refuses
+  // bumped by every reschedule: a batch built from this plan holds device
+  // copies of the schedule's array pointers and refuses to run once it changed
+  uint64_t sched_gen = 0;
   // block grouping: native 64x64 tiles of the outputs sent to plain FP64
   tq::DevArray<int64_t> hyb_tile_start;
   int64_t hyb_tiles = 0;
