@@ -241,8 +241,10 @@ constexpr int OZ_STAG = 5;
 constexpr int OZ_FINAL = 100;
 template <int N>
 struct OzSlots {
-  static constexpr int n = (int)OZ_TMEM_COLS / N >= 2 * OZ_NACC ? 2 * OZ_NACC : OZ_NACC + 1;
+  static constexpr int n = N <= 32 ? 2 * OZ_NACC : N <= 64 ? 2 * OZ_NACC - 1 : OZ_NACC + 1;
   static_assert(n * N <= (int)OZ_TMEM_COLS, "slots exceed TMEM");
+  // A slices held in tensor memory after the slots (8 columns each)
+  static constexpr int ntm = ((int)OZ_TMEM_COLS - n * N) / 8;
 };
 static_assert(OZ_STAG * (OZ_NACC - 1) < OZ_CHUNK, "stagger must fit one chunk");
 
@@ -250,11 +252,19 @@ static_assert(OZ_STAG * (OZ_NACC - 1) < OZ_CHUNK, "stagger must fit one chunk");
 // accumulator min(t+u, OZ_NACC-1) at TMEM column slot[acc].  Descriptors advance
 // by whole row groups (the start-address field counts 16-byte units).  The first
 // product of the k-step into an accumulator whose bit is set in `fresh`
-// overwrites it.
-template <int S, bool FRESH>
+// overwrites it.  A slices t < NTM are copied once into tensor memory (columns
+// acol + 8t) and their products read them there: each A slice is used by up to s
+// products, and reading it from shared memory for every one of them would take
+// most of the shared-memory bandwidth the tensor core has (128 B per clock).
+// The copies are ordered before the MMAs of the same thread, and the MMAs of a
+// k-step before the next k-step's copies.
+template <int S, bool FRESH, int NTM>
 __device__ __forceinline__ void oz_issue(const uint32_t (&col)[OZ_NACC], uint64_t da0,
                                          uint64_t db0, uint32_t a_step, uint32_t b_step,
-                                         uint32_t idesc, uint32_t fresh) {
+                                         uint32_t idesc, uint32_t fresh, uint32_t acol) {
+#pragma unroll
+  for (int t = 0; t < S && t < NTM; t++)
+    tmem_cp_128x256b(acol + 8 * t, da0 + (uint64_t)(t * a_step));
 #pragma unroll
   for (int t = 0; t < S; t++) {
 #pragma unroll
@@ -263,23 +273,27 @@ __device__ __forceinline__ void oz_issue(const uint32_t (&col)[OZ_NACC], uint64_
       // first (t, u) in this order that lands in accumulator acc
       const bool first = acc < OZ_NACC - 1 ? t == 0 : (t == 0 && u == OZ_NACC - 1);
       const uint32_t keep = (FRESH && first && ((fresh >> acc) & 1)) ? 0u : 1u;
-      mma_bf16(col[acc], da0 + (uint64_t)(t * a_step), db0 + (uint64_t)(u * b_step), idesc, keep);
+      if (t < NTM)
+        mma_bf16_ta(col[acc], acol + 8 * t, db0 + (uint64_t)(u * b_step), idesc, keep);
+      else
+        mma_bf16(col[acc], da0 + (uint64_t)(t * a_step), db0 + (uint64_t)(u * b_step), idesc,
+                 keep);
     }
   }
 }
 
-template <bool FRESH>
+template <bool FRESH, int NTM>
 __device__ __forceinline__ void oz_issue_s(int s, const uint32_t (&col)[OZ_NACC], uint64_t da0,
                                            uint64_t db0, uint32_t a_step, uint32_t b_step,
-                                           uint32_t idesc, uint32_t fresh) {
+                                           uint32_t idesc, uint32_t fresh, uint32_t acol) {
   switch (s) {
-    case 1: oz_issue<1, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
-    case 2: oz_issue<2, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
-    case 3: oz_issue<3, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
-    case 4: oz_issue<4, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
-    case 5: oz_issue<5, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
-    case 6: oz_issue<6, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
-    default: oz_issue<7, FRESH>(col, da0, db0, a_step, b_step, idesc, fresh); break;
+    case 1: oz_issue<1, FRESH, NTM>(col, da0, db0, a_step, b_step, idesc, fresh, acol); break;
+    case 2: oz_issue<2, FRESH, NTM>(col, da0, db0, a_step, b_step, idesc, fresh, acol); break;
+    case 3: oz_issue<3, FRESH, NTM>(col, da0, db0, a_step, b_step, idesc, fresh, acol); break;
+    case 4: oz_issue<4, FRESH, NTM>(col, da0, db0, a_step, b_step, idesc, fresh, acol); break;
+    case 5: oz_issue<5, FRESH, NTM>(col, da0, db0, a_step, b_step, idesc, fresh, acol); break;
+    case 6: oz_issue<6, FRESH, NTM>(col, da0, db0, a_step, b_step, idesc, fresh, acol); break;
+    default: oz_issue<7, FRESH, NTM>(col, da0, db0, a_step, b_step, idesc, fresh, acol); break;
   }
 }
 
@@ -503,8 +517,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       }
     }
   } else if (warp == 1) {
-    // ---------------- MMA issuer
-    if (lane == 0) {
+    // ---------------- MMA issuer.  The whole warp runs the loop, so the MMA
+    // operands are warp-uniform values; lane 0 waits on the barriers and one
+    // elected lane (the same one throughout) issues the copies, MMAs and commits.
+    {
+      constexpr uint32_t FULL = 0xffffffffu;
       uint32_t it = 0;
       uint32_t st = 0, ph = 0;  // stage of k-step `it` and its fill parity
       // smem descriptors of stage 0; a stage's are these plus its offset / 16
@@ -523,7 +540,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       // the next tile's record is loaded one tile ahead
       OzTileRec nxt;
       if (blockIdx.x < L.n_tiles) nxt = L.tiles[blockIdx.x];
-      for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
+      for (int64_t t = blockIdx.x; t < L.n_tiles && !__shfl_sync(FULL, abort_flag, 0);
+           t += gridDim.x) {
         const OzTileRec cur = nxt;
         if (t + gridDim.x < L.n_tiles) nxt = L.tiles[t + gridDim.x];
         OzTile T;
@@ -544,36 +562,47 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
 #pragma unroll
         for (int a = 0; a < OZ_NACC; a++) col[a] = tmem + ((map >> (3 * a)) & 7) * N;
         int32_t nk_next = prs[T.seg0].nk;
-        for (int64_t sidx = T.seg0; sidx < T.seg1 && !abort_flag; sidx++) {
+        for (int64_t sidx = T.seg0; sidx < T.seg1 && !__shfl_sync(FULL, abort_flag, 0); sidx++) {
           const int64_t nk = nk_next;
           if (sidx + 1 < T.seg1) nk_next = prs[sidx + 1].nk;
           for (int64_t q = 0; q < nk; q++, it++) {
-            if (!mbar_wait(&full_bar[st], ph)) {
-              atomicOr(L.err, 4);
-              abort_flag = 1;
+            int ok = 1;
+            if (lane == 0) ok = mbar_wait(&full_bar[st], ph);
+            if (!__shfl_sync(FULL, ok, 0)) {
+              if (lane == 0) {
+                atomicOr(L.err, 4);
+                abort_flag = 1;
+              }
               break;
             }
             if (fresh) {
               // a slot taken up again must have been drained since its last use
-              bool ok = true;
+              if (lane == 0) {
 #pragma unroll
-              for (int a = 0; a < OZ_NACC; a++) {
-                const uint32_t p = (map >> (3 * a)) & 7;
-                if (((fresh >> a) & 1) && ((used >> p) & 1) &&
-                    !mbar_wait(&slot_empty[p], ((par >> p) & 1) ^ 1))
-                  ok = false;
+                for (int a = 0; a < OZ_NACC; a++) {
+                  const uint32_t p = (map >> (3 * a)) & 7;
+                  if (((fresh >> a) & 1) && ((used >> p) & 1) &&
+                      !mbar_wait(&slot_empty[p], ((par >> p) & 1) ^ 1))
+                    ok = 0;
+                }
               }
-              if (!ok) {
-                atomicOr(L.err, 8);
-                abort_flag = 1;
+              if (!__shfl_sync(FULL, ok, 0)) {
+                if (lane == 0) {
+                  atomicOr(L.err, 8);
+                  abort_flag = 1;
+                }
                 break;
               }
             }
             tc_fence_after();
             const uint64_t so = (uint64_t)((st * stage_bytes) >> 4);
-            oz_issue_s<true>(s, col, dA0 + so, dB0 + so, (uint32_t)T.ga * 16, (uint32_t)T.gb * 16,
-                             idesc, fresh);
-            mma_commit(&empty_bar[st]);
+            if (elect_one()) {
+              oz_issue_s<true, OzSlots<N>::ntm>(s, col, dA0 + so, dB0 + so, (uint32_t)T.ga * 16,
+                                                (uint32_t)T.gb * 16, idesc, fresh,
+                                                tmem + NSLOT * N);
+              mma_commit(&empty_bar[st]);
+            }
+            __syncwarp();
             if (++st == (uint32_t)NS) {
               st = 0;
               ph ^= 1;
@@ -584,7 +613,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
               for (int a = 0; a < OZ_NACC; a++) {
                 if (a >= n_acc || (ev_kind != OZ_FINAL && a != ev_kind)) continue;
                 const uint32_t p = (map >> (3 * a)) & 7;
-                mma_commit(&slot_full[p]);
+                if (elect_one()) mma_commit(&slot_full[p]);
+                __syncwarp();
                 par ^= 1u << p;
                 used |= 1u << p;
                 // restart a in the oldest free slot; p joins the free list
@@ -603,8 +633,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         }
       }
       // every MMA issued must finish before TMEM is released
-      mma_commit(&done_bar);
-      if (!mbar_wait(&done_bar, 0)) atomicOr(L.err, 32);
+      if (elect_one()) mma_commit(&done_bar);
+      __syncwarp();
+      if (lane == 0 && !mbar_wait(&done_bar, 0)) atomicOr(L.err, 32);
     }
   } else {
     // ---------------- epilogue: 8 warps; warp -> TMEM lane quarter, column half
@@ -687,12 +718,20 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       const int64_t rowB = T.ecol;
       const int32_t *expB = J.expB;
       if (row_ok) {
+        // the column exponents of 8 columns are loaded before their stores, so
+        // the loads are not held behind stores that might alias them
 #pragma unroll
-        for (int y = 0; y < N / 2; y++) {
-          const int64_t gcol = T.nt * N + cbase + y;
-          if (gcol < T.n) {
-            const int fc = expB[rowB + gcol];
-            C[grow + gcol * T.m] = oz_i64_ldexp(S[y], er + fc - 16 - u);
+        for (int y0 = 0; y0 < N / 2; y0 += 8) {
+          int fc[8];
+#pragma unroll
+          for (int y = 0; y < 8; y++) {
+            const int64_t gcol = T.nt * N + cbase + y0 + y;
+            fc[y] = gcol < T.n ? __ldg(expB + rowB + gcol) : 0;
+          }
+#pragma unroll
+          for (int y = 0; y < 8; y++) {
+            const int64_t gcol = T.nt * N + cbase + y0 + y;
+            if (gcol < T.n) C[grow + gcol * T.m] = oz_i64_ldexp(S[y0 + y], er + fc[y] - 16 - u);
           }
         }
       }
