@@ -14,6 +14,8 @@
 // One host synchronisation reads the sizes and allocates the result.
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <vector>
 
 #include "gemm.cuh"
 #include "index.cuh"
@@ -372,6 +374,326 @@ static OzSide make_side(const tq_bs *T, int32_t nfree, const int32_t *fl, int32_
   return S;
 }
 
+// ---------------------------------------------------------------- class layout
+// The (A free box, B free box, pair count) of every output block.
+__global__ void out_xy_kernel(const int32_t *pa, const int32_t *pb, const int64_t *seg,
+                              const int64_t *perm, const int64_t *keyA, const int64_t *keyB,
+                              int64_t n_out, int64_t *xy) {
+  const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= n_out) return;
+  const int64_t p0 = perm ? perm[seg[o]] : seg[o];
+  xy[3 * o] = keyA[pa[p0]];
+  xy[3 * o + 1] = keyB[pb[p0]];
+  xy[3 * o + 2] = seg[o + 1] - seg[o];
+}
+
+template <typename T>
+static tq_status upload(DevArray<T> &d, const std::vector<T> &h, cudaStream_t s) {
+  TQ_CHECK(d.alloc(std::max<size_t>(h.size(), 1), s));
+  if (!h.empty())
+    TQ_CUDA(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  return TQ_OK;
+}
+
+// The class layout of the tensor-core forms (see OzClassOut), built when the
+// contraction admits it: every free box's blocks carry distinct contracted boxes,
+// and any two free boxes (one per side) that share a matched contracted box
+// carry the same set of them.  Sets *used; leaves the plan as it was when the
+// structure does not qualify (the per-block layout then runs).  Runs after the
+// common part of plan_tc (row scans, exponent-table size); replaces the
+// exponent-table offsets rowA / rowB by class order, so that the rows of a
+// class are consecutive in the exponent tables and in its row map.
+static tq_status plan_tc_classes(tq_plan *P, int32_t sl, int32_t tn, int64_t nexpA,
+                                 int64_t nexpB, cudaStream_t s, bool *used) {
+  *used = false;
+  const tq_bs *A = P->A, *B = P->B;
+  const LegSpec &L = P->L;
+  const int64_t no = P->n_out;
+  if (P->opts.layout != TQ_LAYOUT_REDUCED || P->opts.native_fill != 0 || no == 0 || L.nc == 0)
+    return TQ_OK;
+  TQ_CHECK(sync_host_meta(const_cast<tq_bs *>(A), s));
+  TQ_CHECK(sync_host_meta(const_cast<tq_bs *>(B), s));
+  TQ_CHECK(sync_host_meta(P->C, s));
+  const int64_t na = A->nb, nbk = B->nb, KA = P->KA, KB = P->KB;
+  std::vector<int64_t> keyA(na), keyB(nbk), xy(3 * no);
+  {
+    DevArray<int64_t> dxy;
+    TQ_CHECK(dxy.alloc(3 * no, s));
+    count_launch(), out_xy_kernel<<<nblk(no), 256, 0, s>>>(P->pa.p, P->pb.p, P->seg.p, P->perm.p,
+                                                           P->keyA.p, P->keyB.p, no, dxy.p);
+    TQ_CUDA(cudaGetLastError());
+    TQ_CUDA(cudaMemcpyAsync(keyA.data(), P->keyA.p, na * 8, cudaMemcpyDeviceToHost, s));
+    TQ_CUDA(cudaMemcpyAsync(keyB.data(), P->keyB.p, nbk * 8, cudaMemcpyDeviceToHost, s));
+    TQ_CUDA(cudaMemcpyAsync(xy.data(), dxy.p, 3 * no * 8, cudaMemcpyDeviceToHost, s));
+    TQ_CUDA(cudaStreamSynchronize(s));
+  }
+  const int nc = L.nc;
+  // contracted boxes (begin and end on each contracted leg, pair order) -> ids
+  auto coord = [&](int64_t e, int k, int w) -> int64_t {
+    const bool onB = e >= na;
+    const tq_bs *T = onB ? B : A;
+    const int64_t blk = onB ? e - na : e;
+    const int leg = onB ? L.bl[k] : L.al[k];
+    return (w ? T->h_end : T->h_begin)[blk * T->rank + leg];
+  };
+  auto box_less = [&](int64_t x, int64_t y) {
+    for (int k = 0; k < nc; k++)
+      for (int w = 0; w < 2; w++) {
+        const int64_t a = coord(x, k, w), b = coord(y, k, w);
+        if (a != b) return a < b;
+      }
+    return false;
+  };
+  std::vector<int64_t> ord((size_t)(na + nbk));
+  for (int64_t e = 0; e < na + nbk; e++) ord[e] = e;
+  std::sort(ord.begin(), ord.end(), box_less);
+  std::vector<int32_t> boxid((size_t)(na + nbk));
+  std::vector<uint8_t> onA, onB;
+  int32_t nboxes = 0;
+  for (size_t q = 0; q < ord.size(); q++) {
+    if (q == 0 || box_less(ord[q - 1], ord[q])) {
+      nboxes++;
+      onA.push_back(0);
+      onB.push_back(0);
+    }
+    boxid[ord[q]] = nboxes - 1;
+    (ord[q] < na ? onA : onB)[nboxes - 1] = 1;
+  }
+  // signature of every free box: its blocks' matched contracted boxes, sorted
+  typedef std::pair<int32_t, int32_t> BoxBlk;  // (box id, block)
+  std::vector<std::vector<BoxBlk>> sigA((size_t)KA), sigB((size_t)KB);
+  for (int64_t i = 0; i < na; i++)
+    if (onA[boxid[i]] && onB[boxid[i]]) sigA[keyA[i]].push_back(BoxBlk(boxid[i], (int32_t)i));
+  for (int64_t j = 0; j < nbk; j++)
+    if (onA[boxid[na + j]] && onB[boxid[na + j]])
+      sigB[keyB[j]].push_back(BoxBlk(boxid[na + j], (int32_t)j));
+  std::map<std::vector<int32_t>, int32_t> cmap;
+  std::vector<int32_t> clsA((size_t)KA, -1), clsB((size_t)KB, -1);
+  std::vector<std::vector<int32_t>> cboxes;
+  auto classify = [&](std::vector<std::vector<BoxBlk>> &sig, std::vector<int32_t> &cls) {
+    for (size_t x = 0; x < sig.size(); x++) {
+      if (sig[x].empty()) continue;
+      std::sort(sig[x].begin(), sig[x].end());
+      std::vector<int32_t> ids;
+      for (size_t q = 0; q < sig[x].size(); q++) {
+        if (q && sig[x][q].first == sig[x][q - 1].first) return false;  // a box twice
+        ids.push_back(sig[x][q].first);
+      }
+      auto f = cmap.find(ids);
+      if (f == cmap.end()) {
+        f = cmap.emplace(ids, (int32_t)cboxes.size()).first;
+        cboxes.push_back(ids);
+      }
+      cls[x] = f->second;
+    }
+    return true;
+  };
+  if (!classify(sigA, clsA) || !classify(sigB, clsB)) return TQ_OK;
+  // every matched box belongs to one class, the same on both sides
+  std::vector<int32_t> bcA((size_t)nboxes, -1), bcB((size_t)nboxes, -1);
+  auto box_classes = [&](const std::vector<std::vector<BoxBlk>> &sig,
+                         const std::vector<int32_t> &cls, std::vector<int32_t> &bc) {
+    for (size_t x = 0; x < sig.size(); x++)
+      for (const BoxBlk &e : sig[x]) {
+        if (bc[e.first] >= 0 && bc[e.first] != cls[x]) return false;
+        bc[e.first] = cls[x];
+      }
+    return true;
+  };
+  if (!box_classes(sigA, clsA, bcA) || !box_classes(sigB, clsB, bcB)) return TQ_OK;
+  for (int32_t b = 0; b < nboxes; b++)
+    if (bcA[b] != bcB[b]) return TQ_OK;
+  const int64_t ncls = (int64_t)cboxes.size();
+  // members of each class (free boxes in key order) and their sizes
+  auto free_size = [&](const tq_bs *T, int64_t blk, int32_t nf, const int32_t *fl) {
+    int64_t m = 1;
+    for (int q = 0; q < nf; q++)
+      m *= T->h_end[blk * T->rank + fl[q]] - T->h_begin[blk * T->rank + fl[q]] + 1;
+    return m;
+  };
+  std::vector<std::vector<int64_t>> memX((size_t)ncls), memY((size_t)ncls);
+  std::vector<int64_t> posX((size_t)KA, -1), posY((size_t)KB, -1), mX((size_t)KA, 0),
+      nY((size_t)KB, 0);
+  for (int64_t i = 0; i < na; i++) mX[keyA[i]] = free_size(A, i, L.nfa, L.fa);
+  for (int64_t j = 0; j < nbk; j++) nY[keyB[j]] = free_size(B, j, L.nfb, L.fb);
+  for (int64_t x = 0; x < KA; x++)
+    if (clsA[x] >= 0) {
+      posX[x] = (int64_t)memX[clsA[x]].size();
+      memX[clsA[x]].push_back(x);
+    }
+  for (int64_t y = 0; y < KB; y++)
+    if (clsB[y] >= 0) {
+      posY[y] = (int64_t)memY[clsB[y]].size();
+      memY[clsB[y]].push_back(y);
+    }
+  // contracted extent of every box, and k-steps
+  std::vector<int64_t> kbox((size_t)nboxes, 1);
+  for (int64_t e = 0; e < na + nbk; e++) {
+    int64_t k = 1;
+    for (int q = 0; q < nc; q++) k *= coord(e, q, 1) - coord(e, q, 0) + 1;
+    kbox[boxid[e]] = k;
+  }
+  // output block offsets per class and (A box, B box); every pair must be an
+  // output block whose pairs are all the boxes of the class
+  std::vector<int64_t> offs_base((size_t)ncls + 1, 0);
+  for (int64_t c = 0; c < ncls; c++)
+    offs_base[c + 1] = offs_base[c] + (int64_t)memX[c].size() * (int64_t)memY[c].size();
+  if (offs_base[ncls] != no) return TQ_OK;
+  std::vector<int64_t> offs((size_t)no, -1);
+  for (int64_t o = 0; o < no; o++) {
+    const int64_t x = xy[3 * o], y = xy[3 * o + 1], cnt = xy[3 * o + 2];
+    const int32_t c = clsA[x];
+    if (c < 0 || clsB[y] != c || cnt != (int64_t)cboxes[c].size()) return TQ_OK;
+    int64_t &slot = offs[offs_base[c] + posX[x] * (int64_t)memY[c].size() + posY[y]];
+    if (slot >= 0) return TQ_OK;
+    slot = P->C->h_offsets[o];
+  }
+  // the layout: virtual rows / columns, slice storage, slicing work items
+  std::vector<int64_t> rowA((size_t)KA, 0), rowB((size_t)KB, 0);
+  std::vector<OzRowMap> rmA, rmB;
+  std::vector<OzClassItem> itA, itB;
+  std::vector<int32_t> blkA, blkB;
+  std::vector<OzClassOut> out((size_t)ncls);
+  std::vector<int64_t> tstart((size_t)ncls + 1, 0), ksum((size_t)ncls);
+  std::vector<OzPairRec> prs((size_t)ncls);
+  int64_t unitA = 0, unitB = 0, vA = 0, vB = 0;
+  for (int64_t c = 0; c < ncls; c++) {
+    const std::vector<int32_t> &bx = cboxes[c];
+    const int32_t nbox = (int32_t)bx.size();
+    std::vector<int32_t> koff(nbox), nk(nbox);
+    int64_t ks = 0;
+    for (int32_t q = 0; q < nbox; q++) {
+      koff[q] = (int32_t)ks;
+      nk[q] = (int32_t)((kbox[bx[q]] + 15) / 16);
+      ks += nk[q];
+    }
+    if (ks > 0x7fffffff) return TQ_OK;
+    ksum[c] = ks;
+    const int64_t nYc = (int64_t)memY[c].size();
+    // side A: 128-row tiles
+    const int64_t r0 = vA, bbA = (int64_t)blkA.size();
+    for (size_t xi = 0; xi < memX[c].size(); xi++) {
+      const int64_t x = memX[c][xi];
+      rowA[x] = vA;
+      for (int64_t r = 0; r < mX[x]; r++)
+        rmA.push_back(OzRowMap{offs_base[c] + (int64_t)xi * nYc, (int32_t)xi, (int32_t)r,
+                               (int32_t)mX[x], 0});
+      vA += mX[x];
+      for (int32_t q = 0; q < nbox; q++) blkA.push_back(sigA[x][q].second);
+    }
+    const int64_t Mc = vA - r0, tmA = (Mc + OZ_M - 1) / OZ_M;
+    const int64_t u0A = unitA;
+    for (int64_t rt = 0; rt < tmA; rt++) {
+      const int32_t rows = (int32_t)std::min<int64_t>(OZ_M, Mc - rt * OZ_M);
+      for (int32_t q = 0; q < nbox; q++)
+        itA.push_back(OzClassItem{u0A + rt * ks * sl * (OZ_M / 8), r0 + rt * OZ_M, bbA, koff[q],
+                                  nk[q], rows, q, nbox, 0});
+      unitA += ks * sl * ((rows + 7) / 8);
+    }
+    // side B: tile-width column tiles
+    const int64_t c0 = vB, bbB = (int64_t)blkB.size();
+    for (size_t yi = 0; yi < memY[c].size(); yi++) {
+      const int64_t y = memY[c][yi];
+      rowB[y] = vB;
+      for (int64_t r = 0; r < nY[y]; r++)
+        rmB.push_back(OzRowMap{0, (int32_t)yi, (int32_t)r, (int32_t)nY[y], 0});
+      vB += nY[y];
+      for (int32_t q = 0; q < nbox; q++) blkB.push_back(sigB[y][q].second);
+    }
+    const int64_t Nc = vB - c0, tmB = (Nc + tn - 1) / tn;
+    const int64_t u0B = unitB;
+    for (int64_t ct = 0; ct < tmB; ct++) {
+      const int32_t rows = (int32_t)std::min<int64_t>(tn, Nc - ct * tn);
+      for (int32_t q = 0; q < nbox; q++)
+        itB.push_back(OzClassItem{u0B + ct * ks * sl * (tn / 8), c0 + ct * tn, bbB, koff[q],
+                                  nk[q], rows, q, nbox, 0});
+      unitB += ks * sl * ((rows + 7) / 8);
+    }
+    out[c] = OzClassOut{Mc, Nc, r0, c0};
+    tstart[c + 1] = tstart[c] + tmA * tmB;
+    prs[c] = OzPairRec{256 * u0A, 256 * u0B, (int32_t)ks, 0};
+  }
+  // free boxes outside every class keep exponent rows (the exponent pass covers
+  // all blocks) after the class rows
+  for (int64_t x = 0; x < KA; x++)
+    if (clsA[x] < 0) rowA[x] = vA, vA += mX[x];
+  for (int64_t y = 0; y < KB; y++)
+    if (clsB[y] < 0) rowB[y] = vB, vB += nY[y];
+  if (vA != nexpA || vB != nexpB)
+    return fail(TQ_ERR_CUDA, "inconsistent class layout (exponent rows)");
+  TQ_CHECK(upload(P->rowA, rowA, s));
+  TQ_CHECK(upload(P->rowB, rowB, s));
+  TQ_CHECK(upload(P->rmapA, rmA, s));
+  TQ_CHECK(upload(P->rmapB, rmB, s));
+  TQ_CHECK(upload(P->itemsA, itA, s));
+  TQ_CHECK(upload(P->itemsB, itB, s));
+  TQ_CHECK(upload(P->blkA, blkA, s));
+  TQ_CHECK(upload(P->blkB, blkB, s));
+  TQ_CHECK(upload(P->cls_out, out, s));
+  TQ_CHECK(upload(P->cls_offs, offs, s));
+  TQ_CHECK(upload(P->tc_tile_start, tstart, s));
+  TQ_CHECK(upload(P->ksum, ksum, s));
+  TQ_CHECK(upload(P->pair_tab, prs, s));
+  TQ_CHECK(P->expA.alloc(std::max<int64_t>(nexpA, 1), s));
+  TQ_CHECK(P->expB.alloc(std::max<int64_t>(nexpB, 1), s));
+  TQ_CHECK(P->sliceA.alloc(std::max<int64_t>(unitA, 1) * 256, s));
+  TQ_CHECK(P->sliceB.alloc(std::max<int64_t>(unitB, 1) * 256, s));
+  P->classes = true;
+  P->n_cls = ncls;
+  P->tc_tiles = tstart[ncls];
+  P->hyb_tiles = 0;
+  P->tilesA = (int64_t)itA.size();
+  P->tilesB = (int64_t)itB.size();
+  P->tc_side[0] = make_side(A, L.nfa, L.fa, L.nc, L.al, P->keyA.p, P->rowA.p, P->rowstartA.p,
+                            P->tilestartA.p, P->unitA.p);
+  P->tc_side[1] = make_side(B, L.nfb, L.fb, L.nc, L.bl, P->keyB.p, P->rowB.p, P->rowstartB.p,
+                            P->tilestartB.p, P->unitB.p);
+  const int64_t n_rows[2] = {P->rowsA, P->rowsB}, n_items[2] = {P->tilesA, P->tilesB},
+                n_exps[2] = {nexpA, nexpB};
+  int32_t *exps[2] = {P->expA.p, P->expB.p};
+  uint8_t *slices[2] = {P->sliceA.p, P->sliceB.p};
+  const OzClassItem *items[2] = {P->itemsA.p, P->itemsB.p};
+  const OzRowMap *rmaps[2] = {P->rmapA.p, P->rmapB.p};
+  const int32_t *blks[2] = {P->blkA.p, P->blkB.p};
+  for (int k = 0; k < 2; k++) {
+    OzSide &S = P->tc_side[k];
+    S.exps = exps[k];
+    S.slices = slices[k];
+    S.n_rows = n_rows[k];
+    S.n_tiles = n_items[k];
+    S.n_exps = n_exps[k];
+    S.s = sl;
+    S.rt_rows = k == 0 ? OZ_M : tn;
+    S.items = items[k];
+    S.rmap = rmaps[k];
+    S.blk = blks[k];
+  }
+  OzJob &J = P->tc_job;
+  J = OzJob{};
+  J.g = make_gemm_job(P);
+  J.prs = P->pair_tab.p;
+  J.tile_start = P->tc_tile_start.p;
+  J.n_tiles = P->tc_tiles;
+  J.ksum = P->ksum.p;
+  J.sliceA = P->sliceA.p;
+  J.sliceB = P->sliceB.p;
+  J.keyA = P->keyA.p;
+  J.keyB = P->keyB.p;
+  J.rowA = P->rowA.p;
+  J.rowB = P->rowB.p;
+  J.expA = P->expA.p;
+  J.expB = P->expB.p;
+  J.s = sl;
+  J.tile_n = tn;
+  J.cls = P->cls_out.p;
+  J.n_cls = ncls;
+  J.rmapA = P->rmapA.p;
+  J.rmapB = P->rmapB.p;
+  J.offs = P->cls_offs.p;
+  *used = true;
+  return oz_batch_build({J}, {P->tc_side[0], P->tc_side[1]}, s, P->tcb);
+}
+
 static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   const LegSpec &L = P->L;
   const tq_bs *A = P->A, *B = P->B;
@@ -384,6 +706,9 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   if (P->opts.native_fill < 0 || P->opts.native_fill > 1000)
     return fail(TQ_ERR_INVALID, "native_fill outside 0..1000");
   P->tile_n = tn;
+  P->classes = false;
+  P->n_cls = 0;
+  P->tc_job = OzJob{};
   if (KA > (1 << 26) || KB > (1 << 26))
     return fail(TQ_ERR_UNSUPPORTED, "too many distinct free boxes for the sliced forms");
   const int64_t np = P->n_pairs, no = P->n_out;
@@ -455,6 +780,9 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   P->rowsB = h[4];
   P->tilesB = h[5];
   P->nexpB = h[7];
+  bool classes = false;
+  TQ_CHECK(plan_tc_classes(P, sl, tn, P->nexpA, P->nexpB, s, &classes));
+  if (classes) return TQ_OK;
   P->tc_tiles = h[8];
   P->hyb_tiles = h[9];
   if (P->hyb_tiles < 0 || P->hyb_tiles > P->n_tiles)

@@ -133,12 +133,88 @@ __device__ __forceinline__ long long oz_fixed(double x, int shift) {
   return (b >> 63) ? -(long long)q : (long long)q;
 }
 
-// One CTA per (side, block, row tile): slices of all k-steps of the tile.
+// The s slices of k-step q for one half row (8 columns, c = 0 or 1) of row r of
+// an operand row tile with G row groups, written into the k-step's chunk.
+__device__ __forceinline__ void oz_slice_kstep(const double *d, bool row_ok, int64_t ra,
+                                               const Operand &op, int64_t q, int c, int shift,
+                                               int s, int G, int r, uint8_t *chunk) {
+  uint32_t packed[OZ_MAXS][4];
+#pragma unroll
+  for (int t = 0; t < OZ_MAXS; t++)
+#pragma unroll
+    for (int w = 0; w < 4; w++) packed[t][w] = 0;
+#pragma unroll
+  for (int x = 0; x < 8; x++) {
+    const int64_t kk = q * 16 + c * 8 + x;
+    long long F = 0;
+    if (row_ok && kk < op.cols) F = oz_fixed(d[ra + mixed_addr(kk, op.nc, op.cdim, op.cst)], shift);
+    int dig[OZ_MAXS];
+#pragma unroll
+    for (int t = OZ_MAXS - 1; t >= 1; t--) {
+      if (t < s) {
+        const int dd = (int)(((F + 128) & 255) - 128);
+        dig[t] = dd;
+        F = (F - dd) >> 8;
+      } else {
+        dig[t] = 0;
+      }
+    }
+    dig[0] = (int)F;
+#pragma unroll
+    for (int t = 0; t < OZ_MAXS; t++) {
+      // d_t * 2^(-8t), exact in bf16
+      const float v = (float)dig[t] * __int_as_float((127 - 8 * t) << 23);
+      const uint32_t h = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v));
+      packed[t][x >> 1] |= h << (16 * (x & 1));
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < OZ_MAXS; t++) {
+    if (t >= s) break;
+    uint4 v = make_uint4(packed[t][0], packed[t][1], packed[t][2], packed[t][3]);
+    *(uint4 *)(chunk + ((t * G + r / 8) * 2 + c) * 128 + (r % 8) * 16) = v;
+  }
+}
+
+// Class layout: one work item is a row tile of a class times one of its
+// contracted boxes; the tile's rows come from the blocks of several free boxes.
+__device__ __forceinline__ void oz_slice_class(const OzSide &S, int64_t lt) {
+  const OzClassItem it = S.items[lt];
+  const int s = S.s;
+  const int G = (it.rows + 7) / 8;
+  const int r = threadIdx.x >> 1, c = threadIdx.x & 1;
+  if (r >= G * 8) return;
+  const bool row_ok = r < it.rows;
+  Operand op;
+  op.cols = 0;
+  op.nc = 0;
+  int64_t ra = 0;
+  int e = OZ_EXP_ZERO;
+  if (row_ok) {
+    const int64_t vr = it.vrow0 + r;
+    const OzRowMap rm = S.rmap[vr];
+    const int64_t b = S.blk[it.blk_base + (int64_t)rm.xi * it.nbox + it.box];
+    side_operand(S, b, op);
+    ra = op.base + mixed_addr(rm.xr, op.nr, op.rdim, op.rst);
+    e = S.exps[vr];
+  }
+  uint8_t *base = S.slices + 256 * it.unit + (int64_t)it.koff * s * G * 256;
+  const double *d = (const double *)S.T.data;
+  for (int64_t q = 0; q < it.nk; q++)
+    oz_slice_kstep(d, row_ok, ra, op, q, c, 8 * s - e, s, G, r, base + q * (int64_t)s * G * 256);
+}
+
+// One CTA per (side, block, row tile): slices of all k-steps of the tile (or,
+// for a side in the class layout, one CTA per work item).
 __global__ void __launch_bounds__(256) oz_slice_kernel(OzLaunch L) {
   const int64_t g = blockIdx.x;
   const int64_t k = oz_find(L.side_tile_start, L.n_sides, g);
   const OzSide &S = L.sides[k];
   const int64_t lt = g - L.side_tile_start[k];
+  if (S.items) {
+    oz_slice_class(S, lt);
+    return;
+  }
   const int64_t b = oz_find(S.tile_start, S.T.nb, lt);
   const int64_t rt = lt - S.tile_start[b];
   const int s = S.s, rt_rows = S.rt_rows;
@@ -154,47 +230,9 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OzLaunch L) {
   const int64_t grow = rt * rt_rows + r;
   const bool row_ok = r < rows;
   const int e = row_ok ? S.exps[S.row_off[S.key[b]] + grow] : OZ_EXP_ZERO;
-  const int shift = 8 * s - e;
   const int64_t ra = row_ok ? op.base + mixed_addr(grow, op.nr, op.rdim, op.rst) : 0;
-  for (int64_t q = 0; q < nk; q++) {
-    uint8_t *chunk = base + q * (int64_t)s * G * 256;
-    uint32_t packed[OZ_MAXS][4];
-#pragma unroll
-    for (int t = 0; t < OZ_MAXS; t++)
-#pragma unroll
-      for (int w = 0; w < 4; w++) packed[t][w] = 0;
-#pragma unroll
-    for (int x = 0; x < 8; x++) {
-      const int64_t kk = q * 16 + c * 8 + x;
-      long long F = 0;
-      if (row_ok && kk < op.cols) F = oz_fixed(d[ra + mixed_addr(kk, op.nc, op.cdim, op.cst)], shift);
-      int dig[OZ_MAXS];
-#pragma unroll
-      for (int t = OZ_MAXS - 1; t >= 1; t--) {
-        if (t < s) {
-          const int dd = (int)(((F + 128) & 255) - 128);
-          dig[t] = dd;
-          F = (F - dd) >> 8;
-        } else {
-          dig[t] = 0;
-        }
-      }
-      dig[0] = (int)F;
-#pragma unroll
-      for (int t = 0; t < OZ_MAXS; t++) {
-        // d_t * 2^(-8t), exact in bf16
-        const float v = (float)dig[t] * __int_as_float((127 - 8 * t) << 23);
-        const uint32_t h = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v));
-        packed[t][x >> 1] |= h << (16 * (x & 1));
-      }
-    }
-#pragma unroll
-    for (int t = 0; t < OZ_MAXS; t++) {
-      if (t >= s) break;
-      uint4 v = make_uint4(packed[t][0], packed[t][1], packed[t][2], packed[t][3]);
-      *(uint4 *)(chunk + ((t * G + r / 8) * 2 + c) * 128 + (r % 8) * 16) = v;
-    }
-  }
+  for (int64_t q = 0; q < nk; q++)
+    oz_slice_kstep(d, row_ok, ra, op, q, c, 8 * s - e, s, G, r, base + q * (int64_t)s * G * 256);
 }
 // ---------------------------------------------------------------- conversion
 // T * 2^e as a correctly rounded double, integer operations only (the rare
@@ -348,14 +386,25 @@ __device__ __forceinline__ void oz_decode(const OzLaunch &L, int64_t t, OzTile &
   const OzJob &J = L.jobs[j];
   T.J = &J;
   t -= L.job_tile_start[j];
-  T.o = oz_find(J.tile_start, J.g.n_out, t);
-  T.seg0 = J.g.seg[T.o];
-  T.seg1 = J.g.seg[T.o + 1];
-  const int64_t p0 = J.g.perm ? J.g.perm[T.seg0] : T.seg0;
-  T.i0 = J.g.pa[p0];
-  T.j0 = J.g.pb[p0];
-  T.m = free_rows(J.g.A, T.i0, J.g.L.nfa, J.g.L.fa);
-  T.n = free_rows(J.g.B, T.j0, J.g.L.nfb, J.g.L.fb);
+  if (J.cls) {
+    // class layout: output = class, one pseudo-pair per class
+    T.o = oz_find(J.tile_start, J.n_cls, t);
+    const OzClassOut K = J.cls[T.o];
+    T.seg0 = T.o;
+    T.seg1 = T.o + 1;
+    T.i0 = T.j0 = 0;
+    T.m = K.m;
+    T.n = K.n;
+  } else {
+    T.o = oz_find(J.tile_start, J.g.n_out, t);
+    T.seg0 = J.g.seg[T.o];
+    T.seg1 = J.g.seg[T.o + 1];
+    const int64_t p0 = J.g.perm ? J.g.perm[T.seg0] : T.seg0;
+    T.i0 = J.g.pa[p0];
+    T.j0 = J.g.pb[p0];
+    T.m = free_rows(J.g.A, T.i0, J.g.L.nfa, J.g.L.fa);
+    T.n = free_rows(J.g.B, T.j0, J.g.L.nfb, J.g.L.fb);
+  }
   const int64_t tiles_m = (T.m + OZ_M - 1) / OZ_M;
   const int64_t local = t - J.tile_start[T.o];
   T.mt = local % tiles_m;
@@ -380,11 +429,11 @@ __global__ void oz_table_kernel(OzLaunch L, OzTileRec *out) {
   r.seg0 = T.seg0;
   r.seg1 = T.seg1;
   r.ksum = T.ksum;
-  r.c_off = J.g.c_off[T.o];
+  r.c_off = J.cls ? 0 : J.g.c_off[T.o];
   r.m = T.m;
   r.n = T.n;
-  r.erow = J.rowA[J.keyA[T.i0]];
-  r.ecol = J.rowB[J.keyB[T.j0]];
+  r.erow = J.cls ? J.cls[T.o].erow : J.rowA[J.keyA[T.i0]];
+  r.ecol = J.cls ? J.cls[T.o].ecol : J.rowB[J.keyB[T.j0]];
   r.job = (int32_t)(T.J - L.jobs);
   r.mt = (int32_t)T.mt;
   r.nt = (int32_t)T.nt;
@@ -717,7 +766,33 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       double *C = (double *)J.g.C + T.c_off;
       const int64_t rowB = T.ecol;
       const int32_t *expB = J.expB;
-      if (row_ok) {
+      if (J.cls) {
+        // class layout: the tile's rows and columns belong to several output
+        // blocks; each element goes to (its row's A free box, its column's B
+        // free box) at (row within the box) + (column within the box) * rows
+        if (row_ok) {
+          const OzRowMap ra_ = J.rmapA[T.erow + grow];
+#pragma unroll
+          for (int y0 = 0; y0 < N / 2; y0 += 8) {
+            int fc[8];
+            int64_t dst[8];
+#pragma unroll
+            for (int y = 0; y < 8; y++) {
+              const int64_t gcol = T.nt * N + cbase + y0 + y;
+              fc[y] = 0;
+              dst[y] = -1;
+              if (gcol < T.n) {
+                fc[y] = __ldg(expB + rowB + gcol);
+                const OzRowMap cb = J.rmapB[rowB + gcol];
+                dst[y] = __ldg(J.offs + ra_.xoff + cb.xi) + ra_.xr + (int64_t)cb.xr * ra_.m;
+              }
+            }
+#pragma unroll
+            for (int y = 0; y < 8; y++)
+              if (dst[y] >= 0) C[dst[y]] = oz_i64_ldexp(S[y0 + y], er + fc[y] - 16 - u);
+          }
+        }
+      } else if (row_ok) {
         // the column exponents of 8 columns are loaded before their stores, so
         // the loads are not held behind stores that might alias them
 #pragma unroll

@@ -15,6 +15,37 @@ constexpr int OZ_MAXS = 7;       // most slices supported
 constexpr int OZ_MAX_STAGES = 8;
 constexpr int OZ_EXP_ZERO = -(1 << 20);  // exponent of an all-zero row
 
+// Charge-class layout (when the contraction allows it).  Free boxes whose blocks
+// carry the same set of matched contracted boxes form a class; when every pair of
+// free boxes that match at all match on their whole sets, the contraction is a
+// sum over classes of dense products R_c S_c^T, where R_c stacks the rows of all
+// A free boxes of class c and its columns run over the class's contracted boxes
+// (U(1) symmetry gives one class per charge sector).  The sliced operands are
+// then stored per class, and an output tile spans several output blocks, so rows
+// and columns are padded only at the end of a class, not of every block.
+struct OzRowMap {   // one row of a class on one side (a virtual row)
+  int64_t xoff;     // A side: index of the row's free box in the class's output-offset table
+  int32_t xi;       // the row's free box, as its position in the class
+  int32_t xr;       // row within that free box
+  int32_t m;        // rows of that free box
+  int32_t pad;
+};
+
+struct OzClassItem {  // one work item of the class-layout slicing pass
+  int64_t unit;       // slice storage of the row tile, 256-byte units
+  int64_t vrow0;      // first virtual row of the row tile
+  int64_t blk_base;   // the class's entries in blk: [free box * nbox + box]
+  int32_t koff, nk;   // k-step offset of the box within the class, its k-steps
+  int32_t rows;       // rows of the row tile
+  int32_t box, nbox;  // the contracted box, boxes of the class
+  int32_t pad;
+};
+
+struct OzClassOut {  // one class as an output of the GEMM
+  int64_t m, n;      // virtual rows (A side) and columns (B side)
+  int64_t erow, ecol;  // first virtual row / column (also the exponent tables' index)
+};
+
 // One operand side (A or B) of one job, for the slicing passes: every block of
 // the tensor is one operand unit viewed as a rows x k matrix (rows over the
 // free legs, columns over the contracted legs in pair order, each block's full
@@ -32,6 +63,10 @@ struct OzSide {
   uint8_t *slices;            // slice storage
   int64_t n_rows, n_tiles, n_exps;
   int32_t s, rt_rows;
+  // class layout (items != NULL): n_tiles counts the items
+  const OzClassItem *items;
+  const OzRowMap *rmap;       // per virtual row
+  const int32_t *blk;         // block of (free box, contracted box) per class
 };
 
 // One block pair of a job, in the order the GEMM walks them (pairs of each
@@ -56,6 +91,12 @@ struct OzJob {
   const int32_t *expA, *expB;
   int32_t s;
   int32_t tile_n;             // output columns per tile (every job of a launch alike)
+  // class layout (cls != NULL): the GEMM's outputs are the classes, each with one
+  // pseudo-pair (its whole contracted range); tile_start and ksum are per class
+  const OzClassOut *cls;
+  int64_t n_cls;
+  const OzRowMap *rmapA, *rmapB;
+  const int64_t *offs;        // per class and (A free box, B free box): output block offset
 };
 
 // One output tile of a launch, decoded once when the launch is built: the GEMM's

@@ -55,6 +55,14 @@ struct tq_plan {
   int64_t hyb_tiles = 0;
   tq::NativeWorkDev hyb;
   tq::DevArray<tq::OzPairRec> pair_tab;  // pairs in GEMM order (tensor-core forms)
+  // class layout of the tensor-core forms (see OzClassOut)
+  bool classes = false;
+  int64_t n_cls = 0;
+  tq::DevArray<tq::OzClassOut> cls_out;
+  tq::DevArray<tq::OzRowMap> rmapA, rmapB;
+  tq::DevArray<tq::OzClassItem> itemsA, itemsB;
+  tq::DevArray<int32_t> blkA, blkB;
+  tq::DevArray<int64_t> cls_offs;
   tq::OzJob tc_job{};              // this contraction as one job
   tq::OzSide tc_side[2]{};         // its A and B operand sides
   tq::OzBatchDev tcb;              // the same as a batch of one, on the device
