@@ -364,6 +364,38 @@ struct OzSchedule {
   }
 };
 
+// Which TMEM slot each accumulator occupies, replayed identically by the three
+// roles of the GEMM: accumulator a sits in slot bits [3a, 3a+3) of `map`; the
+// free slots wait in `fifo` (3 bits each, oldest retirement first); per slot p,
+// bit p of `par` is the parity of its retirements so far and bit p of `used`
+// whether it had one.
+template <int NSLOT>
+struct OzSlotMap {
+  static constexpr int NFREE = NSLOT - OZ_NACC;
+  uint32_t map, par, used, fifo;
+  __device__ __forceinline__ void init() {
+    map = par = used = fifo = 0;
+#pragma unroll
+    for (int a = 0; a < OZ_NACC; a++) map |= (uint32_t)a << (3 * a);
+#pragma unroll
+    for (int q = 0; q < NFREE; q++) fifo |= (uint32_t)(OZ_NACC + q) << (3 * q);
+  }
+  __device__ __forceinline__ uint32_t slot(int a) const { return (map >> (3 * a)) & 7; }
+  // accumulator a leaves its slot (returned) and restarts in the oldest free one
+  __device__ __forceinline__ uint32_t retire(int a) {
+    const uint32_t p = slot(a);
+    par ^= 1u << p;
+    used |= 1u << p;
+    const uint32_t q = fifo & 7;
+    fifo = (fifo >> 3) | (p << (3 * (NFREE - 1)));
+    map = (map & ~(7u << (3 * a))) | (q << (3 * a));
+    return p;
+  }
+  // parity of the drain that must complete before slot p is written again
+  __device__ __forceinline__ bool needs_drain(uint32_t p) const { return (used >> p) & 1; }
+  __device__ __forceinline__ uint32_t drain_parity(uint32_t p) const { return ((par >> p) & 1) ^ 1; }
+};
+
 // Exact fp32 -> int32 for values whose scaled magnitude is below 2^22 (one FMA
 // against 1.5 * 2^23, whose ulp is 1, then an integer subtract; rounds to
 // nearest even like rint); larger values take the conversion unit.
@@ -515,8 +547,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
   const uint32_t tmem = tmem_base;
 
   if (warp == 0) {
-    // ---------------- producer: one bulk copy per operand per k-step
+    // ---------------- producer: one bulk copy per operand per k-step.  It also
+    // replays the accumulator schedule and, before filling a stage whose MMAs
+    // restart accumulators in TMEM slots used before, waits until the epilogue
+    // has drained those slots: the MMA warp then only waits for its stage (the
+    // stage's completion implies the drain) and keeps feeding the tensor core.
     if (lane == 0) {
+      OzSlotMap<NSLOT> sm;
+      sm.init();
       uint32_t it = 0;
       // stage of k-step `it` and the parity of its previous use (counters, not it % NS)
       uint32_t st = 0, ph = 1;
@@ -534,6 +572,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         const OzPairRec *prs = J.prs;
         const uint8_t *sliceA = J.sliceA, *sliceB = J.sliceB;
         const uint32_t ba = (uint32_t)s * T.ga * 256, bb = (uint32_t)s * T.gb * 256;
+        const int n_acc = s < OZ_NACC ? s : OZ_NACC;
+        OzSchedule sch;
+        sch.start(T.ksum, n_acc);
+        int64_t ev_k;
+        int ev_kind;
+        sch.peek(ev_k, ev_kind);
+        uint32_t fresh = (1u << n_acc) - 1;
+        int64_t k = 0;
         // the next pair's record is loaded one pair ahead
         OzPairRec pn = prs[T.seg0];
         for (int64_t sidx = T.seg0; sidx < T.seg1 && !abort_flag; sidx++) {
@@ -548,6 +594,22 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
               abort_flag = 1;
               break;
             }
+            if (fresh) {
+              bool ok = true;
+#pragma unroll
+              for (int a = 0; a < OZ_NACC; a++) {
+                const uint32_t p = sm.slot(a);
+                if (((fresh >> a) & 1) && sm.needs_drain(p) &&
+                    !mbar_wait(&slot_empty[p], sm.drain_parity(p)))
+                  ok = false;
+              }
+              if (!ok) {
+                atomicOr(L.err, 8);
+                abort_flag = 1;
+                break;
+              }
+              fresh = 0;
+            }
             uint8_t *sa = smem + st * stage_bytes;
             mbar_arrive_expect_tx(&full_bar[st], ba + bb);
             bulk_g2s(sa, ga + q * ba, ba, &full_bar[st]);
@@ -555,6 +617,18 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
             if (++st == (uint32_t)NS) {
               st = 0;
               ph ^= 1;
+            }
+            if (++k == ev_k) {
+#pragma unroll
+              for (int a = 0; a < OZ_NACC; a++) {
+                if (a >= n_acc || (ev_kind != OZ_FINAL && a != ev_kind)) continue;
+                sm.retire(a);
+                fresh |= 1u << a;
+              }
+              if (ev_kind != OZ_FINAL) {
+                sch.advance(ev_kind);
+                sch.peek(ev_k, ev_kind);
+              }
             }
           }
         }
@@ -576,16 +650,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       // smem descriptors of stage 0; a stage's are these plus its offset / 16
       const uint32_t sm0 = smem_u32(smem);
       const uint64_t dA0 = smem_desc(sm0, 128, 256), dB0 = smem_desc(sm0 + a_bytes_max, 128, 256);
-      // slot of accumulator a in bits [3a, 3a+3); per slot p: bit p of `par` is
-      // the parity of its completed uses, bit p of `used` whether it had one
-      uint32_t map = 0, par = 0, used = 0;
-      // free slots, 3 bits each, oldest retirement first (always NSLOT - OZ_NACC)
-      uint32_t fifo = 0;
-      constexpr int NFREE = NSLOT - OZ_NACC;
-#pragma unroll
-      for (int a = 0; a < OZ_NACC; a++) map |= (uint32_t)a << (3 * a);
-#pragma unroll
-      for (int q = 0; q < NFREE; q++) fifo |= (uint32_t)(OZ_NACC + q) << (3 * q);
+      OzSlotMap<NSLOT> sm;
+      sm.init();
       // the next tile's record is loaded one tile ahead
       OzTileRec nxt;
       if (blockIdx.x < L.n_tiles) nxt = L.tiles[blockIdx.x];
@@ -609,7 +675,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         int64_t k = 0;
         uint32_t col[OZ_NACC];
 #pragma unroll
-        for (int a = 0; a < OZ_NACC; a++) col[a] = tmem + ((map >> (3 * a)) & 7) * N;
+        for (int a = 0; a < OZ_NACC; a++) col[a] = tmem + sm.slot(a) * N;
         int32_t nk_next = prs[T.seg0].nk;
         for (int64_t sidx = T.seg0; sidx < T.seg1 && !__shfl_sync(FULL, abort_flag, 0); sidx++) {
           const int64_t nk = nk_next;
@@ -623,25 +689,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
                 abort_flag = 1;
               }
               break;
-            }
-            if (fresh) {
-              // a slot taken up again must have been drained since its last use
-              if (lane == 0) {
-#pragma unroll
-                for (int a = 0; a < OZ_NACC; a++) {
-                  const uint32_t p = (map >> (3 * a)) & 7;
-                  if (((fresh >> a) & 1) && ((used >> p) & 1) &&
-                      !mbar_wait(&slot_empty[p], ((par >> p) & 1) ^ 1))
-                    ok = 0;
-                }
-              }
-              if (!__shfl_sync(FULL, ok, 0)) {
-                if (lane == 0) {
-                  atomicOr(L.err, 8);
-                  abort_flag = 1;
-                }
-                break;
-              }
             }
             tc_fence_after();
             const uint64_t so = (uint64_t)((st * stage_bytes) >> 4);
@@ -661,16 +708,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
 #pragma unroll
               for (int a = 0; a < OZ_NACC; a++) {
                 if (a >= n_acc || (ev_kind != OZ_FINAL && a != ev_kind)) continue;
-                const uint32_t p = (map >> (3 * a)) & 7;
+                const uint32_t p = sm.slot(a);
                 if (elect_one()) mma_commit(&slot_full[p]);
                 __syncwarp();
-                par ^= 1u << p;
-                used |= 1u << p;
-                // restart a in the oldest free slot; p joins the free list
-                const uint32_t q = fifo & 7;
-                fifo = (fifo >> 3) | (p << (3 * (NFREE - 1)));
-                map = (map & ~(7u << (3 * a))) | (q << (3 * a));
-                col[a] = tmem + q * N;
+                sm.retire(a);
+                col[a] = tmem + sm.slot(a) * N;
                 fresh |= 1u << a;
               }
               if (ev_kind != OZ_FINAL) {
@@ -693,14 +735,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
     const int row = 32 * q4 + lane;
     const uint32_t lane_addr = tmem + ((uint32_t)(32 * q4) << 16);
     const int cbase = half * (N / 2);
-    // the MMA warp's slot map, replayed: accumulator a in bits [3a, 3a+3),
-    // bit p of `par` = parity of the drains of slot p so far
-    uint32_t map = 0, par = 0, fifo = 0;
-    constexpr int NFREE = NSLOT - OZ_NACC;
-#pragma unroll
-    for (int a = 0; a < OZ_NACC; a++) map |= (uint32_t)a << (3 * a);
-#pragma unroll
-    for (int q = 0; q < NFREE; q++) fifo |= (uint32_t)(OZ_NACC + q) << (3 * q);
+    // the MMA warp's slot map, replayed
+    OzSlotMap<NSLOT> sm;
+    sm.init();
     for (int64_t t = blockIdx.x; t < L.n_tiles && !abort_flag; t += gridDim.x) {
       OzTile T;
       oz_unpack(L, L.tiles[t], T);
@@ -731,8 +768,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
 #pragma unroll
         for (int a = 0; a < OZ_NACC; a++) {
           if (a >= n_acc || (!done && a != ev_kind)) continue;
-          const uint32_t p = (map >> (3 * a)) & 7;
-          if (!mbar_wait(&slot_full[p], (par >> p) & 1)) {
+          const uint32_t p = sm.slot(a);
+          // the retirement being drained is the (par_p + 1)-th of slot p
+          if (!mbar_wait(&slot_full[p], ((sm.par >> p) & 1))) {
             atomicOr(L.err, 16);
             abort_flag = 1;
             break;
@@ -749,15 +787,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
           tc_fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(&slot_empty[p]);
-          par ^= 1u << p;
 #pragma unroll
           for (int x = 0; x < N / 16; x++)
 #pragma unroll
             for (int y = 0; y < 8; y++)
               S[8 * x + y] += (long long)oz_to_int(__uint_as_float(v[x][y]), scale) << shift;
-          const uint32_t q = fifo & 7;
-          fifo = (fifo >> 3) | (p << (3 * (NFREE - 1)));
-          map = (map & ~(7u << (3 * a))) | (q << (3 * a));
+          sm.retire(a);
           if (!done) sch.advance(a);
         }
       }
