@@ -437,10 +437,18 @@ __device__ __forceinline__ void oz_decode(const OzLaunch &L, int64_t t, OzTile &
     T.m = free_rows(J.g.A, T.i0, J.g.L.nfa, J.g.L.fa);
     T.n = free_rows(J.g.B, T.j0, J.g.L.nfb, J.g.L.fb);
   }
+  // tiles in bands of OZ_BAND row tiles, column tiles in order within a band:
+  // the CTAs working at the same time (consecutive tiles) then share a few row
+  // tiles' A operands and a band's worth of B operands in L2, instead of
+  // streaming one column tile against every row tile of a tall output
   const int64_t tiles_m = (T.m + OZ_M - 1) / OZ_M;
+  const int64_t tiles_n = (T.n + N - 1) / N;
   const int64_t local = t - J.tile_start[T.o];
-  T.mt = local % tiles_m;
-  T.nt = local / tiles_m;
+  const int64_t band = local / (OZ_BAND * tiles_n);
+  const int64_t band_rows = min((int64_t)OZ_BAND, tiles_m - band * OZ_BAND);
+  const int64_t in_band = local - band * OZ_BAND * tiles_n;
+  T.nt = in_band / band_rows;
+  T.mt = band * OZ_BAND + in_band % band_rows;
   const int64_t ra = min((int64_t)OZ_M, T.m - T.mt * OZ_M);
   const int64_t rb = min((int64_t)N, T.n - T.nt * N);
   T.ga = (int32_t)((ra + 7) / 8);

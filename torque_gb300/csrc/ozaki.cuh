@@ -10,6 +10,7 @@ constexpr int OZ_M = 128;        // output rows per tile (A side, TMEM lanes)
 constexpr int OZ_N = 96;         // widest tile: output columns per tile (B side)
 // tile widths the GEMM is instantiated for (the schedule's choice per launch)
 constexpr int OZ_TILE_NS[3] = {32, 64, 96};
+constexpr int OZ_BAND = 8;       // row tiles per band of the tile order
 constexpr int OZ_CHUNK = 21;     // most k-steps of 16 an accumulator holds (K = 336)
 constexpr int OZ_MAXS = 7;       // most slices supported
 constexpr int OZ_MAX_STAGES = 8;
