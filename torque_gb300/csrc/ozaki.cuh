@@ -125,6 +125,7 @@ struct OzLaunch {
   int32_t n_sides;
   int64_t n_rows, n_slice_tiles, n_exps;
   int32_t s_max, nstages, tile_n;
+  int32_t s_all;           // the slice count of every job, or 0 when they differ
   int32_t *err;
   const OzTileRec *tiles;  // [n_tiles]
 };
