@@ -231,11 +231,16 @@ def cpu_sample(c, a_dev, b_dev, seconds, seed=11):
 
 
 # ---------------------------------------------------------------- validation
-def sampled_error(c, a_dev, b_dev, C, n_blocks=6, max_cost=3e9, seed=5):
-    """Max |C - ref| / max|ref| over a seeded sample of output blocks, ref = the
-    sum over the block's pairs of A_i (m x k) @ B_j (k x n) in numpy float64
-    (A's blocks are [a,b | c,d] and B's [c,d | e,f], column-major, so each is
-    that matrix as stored)."""
+def sampled_error(c, a_dev, b_dev, C, n_largest=2, n_random=4, seed=5):
+    """Accuracy on a seeded sample of output blocks: the n_largest blocks by
+    useful work (the longest fused K and widest blocks, where the sliced
+    accumulation is stressed most) and n_random others.  The reference is the
+    sum over the block's pairs of A_i (m x k) @ B_j (k x n) in numpy float64 (A's
+    blocks are [a,b | c,d] and B's [c,d | e,f], column-major, so each is that
+    matrix as stored).  Reports, over the sampled blocks: the normwise error
+    max|C - ref| / max|ref| per block, and the elementwise error against the
+    product of magnitudes, max |C - ref| / (|A||B|) per element (the form the
+    slicing error bound takes)."""
     pa, pb = host_pairs(c)
     fl = pair_flops(c, pa, pb)
     dim, b, e, t, off = C.metadata()
@@ -244,27 +249,42 @@ def sampled_error(c, a_dev, b_dev, C, n_blocks=6, max_cost=3e9, seed=5):
     for q in range(pa.size):
         k = tuple(c.A.begin[pa[q], :2]) + tuple(c.B.begin[pb[q], 2:])
         groups.setdefault(k, []).append(q)
-    cand = [k for k, qs in groups.items() if sum(fl[x] for x in qs) <= max_cost]
+    cost = {k: sum(fl[x] for x in qs) for k, qs in groups.items()}
+    order = sorted(cost, key=lambda k: -cost[k])
+    pick = order[:n_largest]
+    rest = order[n_largest:]
     rng = np.random.default_rng(seed)
-    pick = [cand[x] for x in rng.choice(len(cand), min(n_blocks, len(cand)), replace=False)]
+    pick += [rest[x] for x in rng.choice(len(rest), min(n_random, len(rest)), replace=False)]
     oa, sa = block_offsets(c.A)
     ob, sb = block_offsets(c.B)
-    da, db = c.A.block_dims, c.B.block_dims
-    worst = 0.0
+    da = c.A.block_dims
+    worst, worst_elem, largest_k = 0.0, 0.0, 0
     for k in pick:
         m = int(np.prod(e[:2, keys[k]] - b[:2, keys[k]] + 1))
         n = int(np.prod(e[2:, keys[k]] - b[2:, keys[k]] + 1))
         want = np.zeros((m, n))
+        mag = np.zeros((m, n))
+        kf = 0
         for q in groups[k]:
             i, j = int(pa[q]), int(pb[q])
             kk = int(np.prod(da[i, 2:]))
+            kf += kk
             am = a_dev[int(oa[i]):int(oa[i] + sa[i])].cpu().numpy().reshape((m, kk), order="F")
             bm = b_dev[int(ob[j]):int(ob[j] + sb[j])].cpu().numpy().reshape((kk, n), order="F")
             want += am @ bm
+            mag += np.abs(am) @ np.abs(bm)
+        largest_k = max(largest_k, kf)
         want = want.ravel(order="F")
+        mag = mag.ravel(order="F")
         got = block_data(C, int(off[keys[k]]), m * n)
-        worst = max(worst, float(np.max(np.abs(got - want)) / np.max(np.abs(want))))
-    return worst, len(pick)
+        d = np.abs(got - want)
+        worst = max(worst, float(np.max(d) / np.max(np.abs(want))))
+        worst_elem = max(worst_elem, float(np.max(d / np.maximum(mag, 1e-300))))
+    return {"max_rel_err": worst, "max_elem_err_over_absAB": worst_elem, "blocks": len(pick),
+            "largest_fused_k": largest_k,
+            "vs": "numpy float64 block products: the %d largest output blocks by useful work and "
+                  "%d random ones (seed %d); max_rel_err is max|C-ref|/max|ref| per block" %
+                  (n_largest, len(pick) - n_largest, seed)}
 
 
 def block_data(C, offset, n):
@@ -305,10 +325,14 @@ def run_reference(args):
         if s >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
+    ref_config = config_dict(args, c)
+    # the reference's CPU path computes in plain FP64 (no slicing)
+    ref_config.update({"pairs": int(host_pairs(c)[0].size), "precision": "fp64 (host CPU)",
+                       "slices": None})
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": config_dict(args, c),
+            "data": "synthetic", "config": ref_config,
             "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
                              "sample": "per step: " + desc},
             "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
@@ -426,7 +450,8 @@ def run_ours(args):
         g_ms = statistics.mean(gemm_ms)
         if args.precision == "native":
             roof = {"bound": "fp64", "achieved": flops / (g_ms / 1e3) / 1e12,
-                    "peak": 1.25, "unit": "TFLOP/s", "peak_source": "nominal FP64"}
+                    "peak": fp64_peak(), "unit": "TFLOP/s",
+                    "peak_source": "measured: cuBLAS DGEMM (torch.matmul float64 8192^3)"}
         else:
             ach = flops * nprod / (g_ms / 1e3) / 1e12
             roof = {"bound": "tensor", "achieved": ach, "peak": pk["bf16_sustained"],
@@ -446,34 +471,38 @@ def run_ours(args):
                 roof["traffic"] = ent["bytes_per_launch"]
         line["roofline"] = roof
 
+        if not args.no_e2e:
+            # right after the device-resident steps, in the same GPU state (the
+            # device-resident inputs stay allocated for the legs below)
+            ah, bh, ch = pinned
+            ah.copy_(a)
+            bh.copy_(b)
+            torch.cuda.synchronize()
+            line["e2e"] = e2e(tq, c, ah, bh, kw, 3, ch)
+            line["e2e"]["host_cores"] = ("%d cores local to the GPU" % len(near)) if near else \
+                "unbound"
+            del ah, bh, ch, pinned
+            _lib.check(lib.tq_release_cached_memory())
+
         # accuracy on sampled output blocks (outside the timed region)
         P, _ = step()
-        err, nb = sampled_error(c, a, b, P.result)
-        line["error"] = {"max_rel_err": err, "blocks": nb,
-                         "vs": "numpy float64 block products on sampled output blocks (each "
-                               "block's max |C| as the scale)"}
+        line["error"] = sampled_error(c, a, b, P.result)
         del P
 
         if not args.no_fp64:
-            line["plain_fp64"] = fp64_subset(tq, c, A, a, b, kw)
+            P, _ = step()
+            line["plain_fp64"] = fp64_full(tq, c, A, B, P.result)
+            # the whole sliced step (plan, operand slicing, GEMM) against the FP64
+            # numeric stage alone
+            line["plain_fp64"]["speedup_step_vs_fp64_numeric"] = \
+                line["plain_fp64"]["numeric_ms"] / ms
+            del P
         if not args.no_hbm:
             line["hbm_kernels"] = hbm_kernels(tq, c, A, B)
         line["cpu_baseline"] = dict(zip(("value", "cores", "sample"),
                                         cpu_sample(c, a, b, args.cpu_seconds)))
         line["cpu_baseline"].update({"unit": "TFLOP/s", "kind": "port"})
 
-        if not args.no_e2e:
-            # right after the device-resident steps, in the same GPU state
-            ah, bh, ch = pinned
-            ah.copy_(a)
-            bh.copy_(b)
-            del A, B, a, b
-            torch.cuda.empty_cache()
-            _lib.check(lib.tq_release_cached_memory())  # a fresh pool for the e2e passes
-            line["e2e"] = e2e(tq, c, ah, bh, kw, 3, ch)
-            line["e2e"]["host_cores"] = ("%d cores local to the GPU" % len(near)) if near else \
-                "unbound"
-            del ah, bh, ch, pinned
         _lib.check(lib.tq_release_cached_memory())
 
         if not args.no_sweep:
@@ -535,55 +564,67 @@ def tune_name(c):
     return "s%d/n%d/g%d" % (c["slices"], c["tile_n"], c["native_fill"])
 
 
-def fp64_subset(tq, c, A, a, b, kw):
-    """Plain FP64 (native) and the chosen form on the same sub-workload: B
-    restricted to every 8th output sector (e,f), so the block-size mix of the
-    full case is kept."""
+def fp64_peak():
+    """FP64 rate of this GPU as cuBLAS DGEMM delivers it (torch.matmul of two
+    8192 x 8192 float64 matrices, best of 3, CUDA events): the roofline
+    denominator of the plain FP64 form."""
     import torch
-    keys = sorted({tuple(x) for x in c.B.begin[:, 2:]})
-    keep = set(keys[::8])
-    sel = np.asarray([j for j in range(c.B.n_blocks) if tuple(c.B.begin[j, 2:]) in keep])
-    ob, sb = block_offsets(c.B)
-    parts = [b[int(ob[j]):int(ob[j] + sb[j])] for j in sel]
-    bsub = torch.cat(parts)
-    Bs = tq.BlockSparseTensor(c.B.dimension, bsub, c.B.begin[sel].T, c.B.end[sel].T)
-    res = {}
-    for name, opts in (("fp64", dict(precision="native", layout="reduced")), ("form", kw)):
-        P = tq.ContractionPlan(A, Bs, c.pairs, **opts)
-        P.execute()
-        P.check()
+    n = 8192
+    x = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    y = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(x, y)
+    best = None
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(x, y)
+        e1.record()
         torch.cuda.synchronize()
-        t = time.perf_counter()
-        P = tq.ContractionPlan(A, Bs, c.pairs, **opts)
-        P.execute()
-        P.check()
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t
-        res[name] = P.flops / dt / 1e12
-        fl = P.flops
-        # compared on the device (no multi-GB host copies)
-        dev = _ptr_tensor(P.result.device_ptr(), P.result.n_elem)
-        if name == "fp64":
-            ref = dev.clone()
-        else:
-            res["form_vs_fp64_max_rel_diff"] = float(torch.max(torch.abs(dev - ref)) /
-                                                     torch.max(torch.abs(ref)))
-        del P, dev
-    del ref, Bs, bsub
-    return {"value": res["fp64"], "unit": "TFLOP/s", "form_value": res["form"],
-            "speedup": res["form"] / res["fp64"],
-            "form_vs_fp64_max_rel_diff": res["form_vs_fp64_max_rel_diff"],
-            "sample": "B restricted to every 8th (e,f) sector: %d of %d blocks, %.3g useful flop, "
-                      "one full contraction each" % (sel.size, c.B.n_blocks, fl)}
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    del x, y
+    torch.cuda.empty_cache()
+    return 2.0 * n ** 3 / (best / 1e3) / 1e12
 
 
-def sweep(tq, n=256, forms=(("ozaki", 5), ("bf16x3", 3)), replays=20):
+def fp64_full(tq, c, A, B, form_result):
+    """Plain FP64 (the native form) on the whole workload: the plan (symbolic
+    stage) timed by wall clock, the numeric stage by CUDA events on the launching
+    stream; its result compared on the device with the sliced form's."""
+    import torch
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    P = tq.ContractionPlan(A, B, c.pairs, precision="native", layout="reduced")
+    torch.cuda.synchronize()
+    plan_ms = (time.perf_counter() - t) * 1e3
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    P.execute()
+    e1.record()
+    P.check()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    ref = _ptr_tensor(P.result.device_ptr(), P.result.n_elem)
+    got = _ptr_tensor(form_result.device_ptr(), form_result.n_elem)
+    diff = float(torch.max(torch.abs(got - ref)) / torch.max(torch.abs(ref)))
+    fl = P.flops
+    del P, ref, got
+    peak = fp64_peak()
+    return {"value": fl / (ms / 1e3) / 1e12, "unit": "TFLOP/s", "numeric_ms": ms,
+            "plan_ms": plan_ms, "useful_flop": fl, "form_vs_fp64_max_rel_diff": diff,
+            "fp64_peak_tflops": peak, "frac_of_fp64_peak": fl / (ms / 1e3) / 1e12 / peak,
+            "peak_source": "cuBLAS DGEMM via torch.matmul float64 8192^3, best of 3",
+            "sample": "the whole workload, one contraction"}
+
+
+def sweep(tq, n=256, forms=(("native", 0), ("ozaki", 5), ("bf16x3", 3)), replays=20):
     """PEPS-sweep site updates (E1 x T over (l,u), then X x E2 over (chi',r,d);
-    D ~ U{4..10}, chi ~ U{16..64}, seed 3): n sequential plain-FP64 contract
-    calls (symbolic + numeric each, as the reference runs them) against the same
-    contractions planned once and run as one replayed CUDA graph of the batched
-    sliced form (one persistent GEMM launch per wave), for the FP64-level
-    (Ozaki) and the FP32-level (3 x bf16) forms."""
+    D ~ U{4..10}, chi ~ U{16..64}, seed 3), every form run the same way: the 2n
+    contractions planned once (symbolic stage, timed), then the numeric stage of
+    all of them as one batch (tensor-core plans of a wave in one persistent
+    launch) captured as a CUDA graph and replayed (timed with CUDA events); plus
+    the reference's way for plain FP64, n sequential contract calls (symbolic +
+    numeric each).  Errors of the sliced forms against the plain FP64 batch."""
     import torch
     from torque_gb300 import workloads
     inst = workloads.peps_sweep(n, seed=3)
@@ -604,11 +645,12 @@ def sweep(tq, n=256, forms=(("ozaki", 5), ("bf16x3", 3)), replays=20):
 
     sequential()
     t = time.perf_counter()
-    ref = sequential()
+    sequential()
     t_seq = time.perf_counter() - t
     res = {"instances": n, "sequential_fp64_ms": t_seq * 1e3}
+    pk = measured_peaks()
+    ref = None
     for precision, slices in forms:
-        # plans: the symbolic stage once
         t = time.perf_counter()
         p1 = [tq.ContractionPlan(E1, T, s.pairs1, precision=precision, slices=slices,
                                  layout="reduced") for s, (T, E1, E2) in zip(inst, ts)]
@@ -628,17 +670,26 @@ def sweep(tq, n=256, forms=(("ozaki", 5), ("bf16x3", 3)), replays=20):
         torch.cuda.synchronize()
         batch.check()
         t_graph = ev0.elapsed_time(ev1) / 1e3 / replays
-        err = 0.0
-        for a, b in zip(p2, ref):
-            x, y = a.result.data(), b.data()
-            err = max(err, float(np.max(np.abs(x - y)) / np.max(np.abs(y))))
+        outs = [p.result.data().copy() for p in p2]
+        ent = {"slices": slices or None, "plan_ms_once": t_plan * 1e3, "graph_ms": t_graph * 1e3,
+               "graph_tflops": flops / t_graph / 1e12, "plan_plus_run_ms": (t_plan + t_graph) * 1e3,
+               "graph_kernels": batch.kernels}
+        if precision == "native":
+            ref = outs
+        else:
+            nprod = slices * (slices + 1) // 2
+            ent["slice_product_tflops"] = flops * nprod / t_graph / 1e12
+            ent["frac_of_bf16_sustained"] = ent["slice_product_tflops"] / pk["bf16_sustained"]
+            ent["max_rel_err_vs_fp64"] = max(float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
+                                              for x, y in zip(outs, ref))
+            ent["speedup_vs_fp64_batched"] = res["native"]["graph_ms"] / (t_graph * 1e3)
+            ent["speedup_plan_plus_run_vs_fp64"] = (res["native"]["plan_plus_run_ms"] /
+                                                    ent["plan_plus_run_ms"])
+            ent["speedup_vs_sequential_fp64"] = t_seq / t_graph
+        res[precision] = ent
         res["useful_flop"] = flops
-        res["sequential_fp64_tflops"] = flops / t_seq / 1e12
-        res[precision] = {"slices": slices, "graph_ms": t_graph * 1e3,
-                          "graph_tflops": flops / t_graph / 1e12, "speedup": t_seq / t_graph,
-                          "plan_ms_once": t_plan * 1e3, "graph_kernels": batch.kernels,
-                          "max_rel_err_vs_fp64": err}
         del batch, p1, p2
+    res["sequential_fp64_tflops"] = res["useful_flop"] / t_seq / 1e12
     return res
 
 
@@ -669,7 +720,7 @@ def peps_norm(tq):
     return out
 
 
-def cost_model(tq, n_live=24):
+def cost_model(tq, n_live=200):
     """The learned cost model: trained on the GPU (library kernels) on the
     exhaustive tuner's measurements of 1,800 random contractions (seed 4),
     evaluated on the 200 held-out ones: regret against exhaustive tuning and gain
@@ -694,27 +745,55 @@ def cost_model(tq, n_live=24):
         rep["%g" % eps] = {"model": m, "default": d,
                            "gain_over_default": d["ms_total"] / m["ms_total"]}
     out["held_out"] = rep
-    # live: the proposal at 1e-10 run and checked against plain FP64 on the device
-    specs = cm.held_out_specs()
-    live_fl, live_ms, live_fp64, worst = 0.0, 0.0, 0.0, 0.0
-    for sp in specs[:n_live]:
+    # live: the model's proposals at 1e-10 for the held-out contractions, all of
+    # them as one batch replayed as a CUDA graph, against the plain FP64 form
+    # batched the same way; every result checked against its FP64 result
+    specs = cm.held_out_specs()[:n_live]
+    keep, prop, nat = [], [], []
+    for sp in specs:
         rc = workloads.from_spec(sp)
         A, B, P = cm.plan_random(rc, 4)
-        f = P.features(1e-10)
-        pick = int(net.propose(f)[0])
-        best, ent = P.autotune(1e-10, [cm.CANDIDATES[pick], dict(precision="native")], reps=3)
-        if ent[0][2] > 1e-10 or ent[0][0] != 0:  # the tuner is the fallback
-            best, ent2 = P.autotune(1e-10, cm.CANDIDATES, reps=1)
-            ent[0] = ent2[best]
-        live_fl += P.flops
-        live_ms += ent[0][1]
-        live_fp64 += ent[1][1]
-        worst = max(worst, ent[0][2])
-        del A, B, P
-    out["live"] = {"contractions": min(n_live, len(specs)), "useful_flop": live_fl,
-                   "tflops_model": live_fl / live_ms / 1e9, "tflops_fp64": live_fl / live_fp64 / 1e9,
-                   "speedup_vs_fp64": live_fp64 / live_ms, "max_rel_err_vs_fp64": worst,
-                   "timing": "numeric stage, fastest of 3 after a warm-up, CUDA events"}
+        pick = cm.CANDIDATES[int(net.propose(P.features(1e-10))[0])]
+        if pick["precision"] == "native":
+            P.reschedule("native")
+        else:
+            P.reschedule(pick["precision"], slices=pick["slices"], tile_n=pick["tile_n"],
+                         native_fill=pick["native_fill"])
+        N = tq.ContractionPlan(A, B, rc.pairs, precision="native", layout="reduced")
+        keep.append((A, B))
+        prop.append(P)
+        nat.append(N)
+
+    def replay(plans, reps=10):
+        b = tq.Batch(plans)
+        b.graph_launch()
+        b.check()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            b.graph_launch()
+        e1.record()
+        torch.cuda.synchronize()
+        b.check()
+        return e0.elapsed_time(e1) / reps, b.kernels
+
+    ms_model, k_model = replay(prop)
+    ms_fp64, k_fp64 = replay(nat)
+    worst = 0.0
+    for P, N in zip(prop, nat):
+        x = _ptr_tensor(P.result.device_ptr(), P.result.n_elem)
+        y = _ptr_tensor(N.result.device_ptr(), N.result.n_elem)
+        if P.result.n_elem:
+            worst = max(worst, float(torch.max(torch.abs(x - y)) / torch.max(torch.abs(y))))
+    fl = sum(P.flops for P in prop)
+    out["live"] = {"contractions": len(specs), "useful_flop": fl,
+                   "tflops_model": fl / ms_model / 1e9, "tflops_fp64": fl / ms_fp64 / 1e9,
+                   "speedup_vs_fp64": ms_fp64 / ms_model, "max_rel_err_vs_fp64": worst,
+                   "graph_kernels_model": k_model, "graph_kernels_fp64": k_fp64,
+                   "timing": "all held-out contractions as one batch (the model's proposals at "
+                             "1e-10), CUDA-graph replay, CUDA events, mean of 10; plain FP64 "
+                             "batched and replayed the same way"}
+    del keep, prop, nat
     return out
 
 
