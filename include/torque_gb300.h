@@ -46,7 +46,12 @@ typedef enum {
   TQ_ERR_TIMEOUT = 6      /* a bounded device wait gave up */
 } tq_status;
 
-typedef enum { TQ_F32 = 0, TQ_F64 = 1 } tq_dtype;
+/* Element types: the reference instantiates float, double and half
+ * (src/gpu/block_sparse.cu:66-148).  TQ_F16 is IEEE binary16; its native
+ * contraction accumulates every output element in FP32 and rounds it to
+ * binary16 once (the reference's cublasHgemm path, block_sparse.cuh:894-930,
+ * accumulates in half).  The tensor-core forms take TQ_F64 only. */
+typedef enum { TQ_F32 = 0, TQ_F64 = 1, TQ_F16 = 2 } tq_dtype;
 
 typedef enum { TQ_MEM_HOST = 0, TQ_MEM_DEVICE = 1 } tq_memkind;
 
@@ -344,6 +349,14 @@ void tq_debug_fail_alloc_after(int64_t after);
 
 /* Kernels the library has launched in this process so far. */
 int64_t tq_debug_kernel_launches(void);
+/* Failure-path test hook of the tensor-core forms: the launches built from now
+ * on (plan creation, reschedule, batch creation) give up every pipeline wait
+ * after wait_ns nanoseconds of wall time (0 = the default, 2 s) and hold their
+ * producer back for producer_delay_ns before it issues anything (0 = none).
+ * With a delay well above the limit, the waiting roles give up, the kernel
+ * drains and frees its tensor memory, and the next check returns
+ * TQ_ERR_TIMEOUT; nothing is left in flight.  Reset with (0, 0). */
+void tq_debug_set_waits(uint64_t wait_ns, uint64_t producer_delay_ns);
 
 #ifdef __cplusplus
 }

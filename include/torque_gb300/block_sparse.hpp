@@ -24,6 +24,8 @@
 #include <stdexcept>
 #include <string>
 #include <type_traits>
+
+#include <cuda_fp16.h>
 #include <utility>
 #include <vector>
 
@@ -65,9 +67,10 @@ inline std::vector<int64_t> flat(const arma::umat &m) {
 
 template <typename T>
 constexpr tq_dtype dtype() {
-  static_assert(std::is_same<T, float>::value || std::is_same<T, double>::value,
-                "torque_gb300 supports float and double tensors");
-  return std::is_same<T, float>::value ? TQ_F32 : TQ_F64;
+  static_assert(std::is_same<T, float>::value || std::is_same<T, double>::value ||
+                    std::is_same<T, __half>::value,
+                "torque_gb300 supports float, double and half tensors");
+  return std::is_same<T, float>::value ? TQ_F32 : std::is_same<T, double>::value ? TQ_F64 : TQ_F16;
 }
 
 inline tq_memkind kind_of(cudaMemcpyKind k) {

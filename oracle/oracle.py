@@ -266,3 +266,34 @@ def assemble_dense(dimension, begin, end, offsets, data) -> np.ndarray:
 
 if __name__ == "__main__":  # pragma: no cover
     print(build(force="--force" in sys.argv))
+
+
+def slice_boxes(begin, end, divisor):
+    """Restates BlockSparseTensor::slice (src/gpu/block_sparse.cuh:1124-1176): every
+    block (rows of begin/end, [n_blocks, rank]) is cut into prod(divisor)
+    sub-boxes of block_dim / divisor per leg, numbered with leg 0 fastest
+    (index_to_indices over generate_index_table(divisor), src/util/space.h:11-45),
+    blocks in order.  A block dimension that the divisor does not divide raises
+    ValueError ("current slice does not support residues").  The data are not
+    moved: the new tensor reads the old buffer through each sub-box's own
+    column-major strides."""
+    begin = np.asarray(begin, np.int64)
+    end = np.asarray(end, np.int64)
+    divisor = np.asarray(divisor, np.int64)
+    dims = end - begin + 1
+    if np.any(dims % divisor):
+        raise ValueError("current slice does not support residues")
+    sub = dims // divisor
+    nsub = int(np.prod(divisor))
+    nb, ne = [], []
+    for i in range(begin.shape[0]):
+        for j in range(nsub):
+            idx, t = [], j
+            for d in divisor:
+                idx.append(t % d)
+                t //= d
+            b = begin[i] + np.asarray(idx) * sub[i]
+            nb.append(b)
+            ne.append(b + sub[i] - 1)
+    return np.asarray(nb, np.int64).reshape(-1, begin.shape[1]), \
+        np.asarray(ne, np.int64).reshape(-1, begin.shape[1])

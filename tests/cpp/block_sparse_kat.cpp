@@ -1,6 +1,7 @@
 // The reference's known answers (test/gpu/block_sparse_test.cu:10-231) run
 // through the C++ drop-in class torque::gpu::BlockSparseTensor<T>, written the
-// way a reference user writes them.  Exit status = number of failed checks.
+// way a reference user writes them, for T = float, double and half (the
+// reference's instantiations, src/gpu/block_sparse.cu:66-148).  Exit status = number of failed checks.
 #include <cstdio>
 #include <vector>
 
@@ -15,6 +16,11 @@ static int g_failed = 0;
     }                                                                  \
   } while (0)
 
+// values compared as float or double (binary16 has no built-in comparison on the host)
+static float val(float x) { return x; }
+static double val(double x) { return x; }
+static float val(__half x) { return __half2float(x); }
+
 template <typename T>
 void run_cases() {
   using torque::gpu::BlockSparseTensor;
@@ -23,33 +29,33 @@ void run_cases() {
   {  // matrix: init, query, modify, append
     std::vector<T> a = {1, 2, 3, 4};
     BlockSparseTensor<T> t(a.data(), arma::uvec{1, 1}, arma::uvec{2, 2}, arma::uvec{4, 3});
-    EXPECT(t.query({1, 1}) == 1);
-    EXPECT(t.query({2, 2}) == 4);
-    EXPECT(t.query({3, 2}) == 0);
+    EXPECT(val(t.query({1, 1})) == 1);
+    EXPECT(val(t.query({2, 2})) == 4);
+    EXPECT(val(t.query({3, 2})) == 0);
     t.modify({2, 2}, 0);
-    EXPECT(t.query({2, 2}) == 0);
+    EXPECT(val(t.query({2, 2})) == 0);
     t.modify({3, 2}, 5);
-    EXPECT(t.query({3, 2}) == 5);
+    EXPECT(val(t.query({3, 2})) == 5);
     t.append_block(a.data(), {0, 0}, {1, 1}, {1, 2});
-    EXPECT(t.query({1, 1}) == 5);
+    EXPECT(val(t.query({1, 1})) == 5);
     EXPECT(t.block_offsets.n_elem == 3);
   }
   {  // matrix transposition
     std::vector<T> a = {1, 2, 3, 4};
     BlockSparseTensor<T> t(a.data(), arma::uvec{2, 0}, arma::uvec{3, 1}, arma::uvec{4, 3});
     t = t.hard_transpose({1, 0});
-    EXPECT(t.query({0, 3}) == 2);
-    EXPECT(t.query({1, 2}) == 3);
+    EXPECT(val(t.query({0, 3})) == 2);
+    EXPECT(val(t.query({1, 2})) == 3);
     const auto back = t.hard_transpose({1, 0});
-    EXPECT(back.query({3, 0}) == 2);
-    EXPECT(back.query({2, 1}) == 3);
+    EXPECT(val(back.query({3, 0})) == 2);
+    EXPECT(val(back.query({2, 1})) == 3);
   }
   {  // rank-3 tensor: empty, then one appended block
     BlockSparseTensor<T> t(arma::uvec{2, 2, 3});
-    EXPECT(t.query({1, 1, 0}) == 0);
+    EXPECT(val(t.query({1, 1, 0})) == 0);
     std::vector<T> a = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12};
     t.append_block(a.data(), {0, 0, 0}, {1, 1, 2}, {1, 2, 4});
-    EXPECT(t.query({0, 1, 2}) == 11);
+    EXPECT(val(t.query({0, 1, 2})) == 11);
   }
   {  // rank-3 transposition with overlapping blocks
     std::vector<T> a = {1, 2, 3, 4, 5, 6, 0, 0, 0, 0, 0, 0};
@@ -58,23 +64,23 @@ void run_cases() {
     t.append_block(a.data(), {0, 0, 0}, {1, 1, 2}, {1, 2, 4});
     t.append_block(b.data(), {1, 0, 0}, {1, 1, 2}, {1, 1, 2});
     const auto p = t.hard_transpose({1, 0, 2});
-    EXPECT(p.query({1, 0, 0}) == 3);
-    EXPECT(p.query({1, 0, 1}) == 0);
-    EXPECT(p.query({1, 1, 2}) == 12);
+    EXPECT(val(p.query({1, 0, 0})) == 3);
+    EXPECT(val(p.query({1, 0, 1})) == 0);
+    EXPECT(val(p.query({1, 1, 2})) == 12);
   }
   {  // scalar
     BlockSparseTensor<T> t(arma::uvec{});
     EXPECT(t.rank == 0);
-    EXPECT(t.query({}) == 0);
+    EXPECT(val(t.query({})) == 0);
     t.modify({}, 1);
-    EXPECT(t.query({}) == 1);
+    EXPECT(val(t.query({})) == 1);
   }
   {  // vector with itself -> 30
     std::vector<T> v1{0, 1}, v2{2, 3, 4};
     BlockSparseTensor<T> t(arma::uvec{5});
     t.append_block(v1.data(), {0}, {1}, {1});
     t.append_block(v2.data(), {2}, {4}, {1});
-    EXPECT(t.contract(handle, t, arma::umat({{0, 0}})).to_number() == 30);
+    EXPECT(val(t.contract(handle, t, arma::umat({{0, 0}})).to_number()) == 30);
   }
   {  // block-diagonal matrix squared
     std::vector<T> b1{0, 1, 2, 3}, b2{4, 5, 6, 7};
@@ -84,14 +90,14 @@ void run_cases() {
     const auto sq = t.contract(handle, t, arma::umat({1, 0}));
     const T want[4][4] = {{2, 6, 0, 0}, {3, 11, 0, 0}, {0, 0, 46, 66}, {0, 0, 55, 79}};
     for (arma::uword i = 0; i < 4; i++)
-      for (arma::uword j = 0; j < 4; j++) EXPECT(sq.query({i, j}) == want[i][j]);
+      for (arma::uword j = 0; j < 4; j++) EXPECT(val(sq.query({i, j})) == val(want[i][j]));
   }
   {  // matrix inner product over both legs -> 206
     std::vector<T> b1{0, 1, 2, 3}, b2{0, 7, 8, 9};
     BlockSparseTensor<T> t(arma::uvec{3, 3});
     t.append_block(b1.data(), {0, 0}, {1, 1}, {1, 2});
     t.append_block(b2.data(), {1, 1}, {2, 2}, {1, 2});
-    EXPECT(t.contract(handle, t, arma::umat{{1, 0}, {0, 1}}).to_number() == 206);
+    EXPECT(val(t.contract(handle, t, arma::umat{{1, 0}, {0, 1}}).to_number()) == 206);
   }
   {  // tensor-vector over each leg
     std::vector<T> d1{0, 1, 2, 3}, d2{4, 5, 6, 7}, v{1, 2};
@@ -101,13 +107,13 @@ void run_cases() {
     BlockSparseTensor<T> vec(arma::uvec{2});
     vec.append_block(v.data(), {0}, {1}, {1});
     const auto c0 = t.contract(handle, vec, arma::umat{{0, 0}});
-    EXPECT(c0.query({0, 0}) == 2 && c0.query({1, 0}) == 8);
-    EXPECT(c0.query({0, 1}) == 14 && c0.query({1, 1}) == 20);
+    EXPECT(val(c0.query({0, 0})) == 2 && val(c0.query({1, 0})) == 8);
+    EXPECT(val(c0.query({0, 1})) == 14 && val(c0.query({1, 1})) == 20);
     const auto c1 = t.contract(handle, vec, arma::umat{{1, 0}});
-    EXPECT(c1.query({0, 0}) == 4 && c1.query({1, 0}) == 7);
-    EXPECT(c1.query({0, 1}) == 16 && c1.query({1, 1}) == 19);
+    EXPECT(val(c1.query({0, 0})) == 4 && val(c1.query({1, 0})) == 7);
+    EXPECT(val(c1.query({0, 1})) == 16 && val(c1.query({1, 1})) == 19);
     const auto c2 = t.contract(handle, vec, arma::umat{{2, 0}});
-    EXPECT(c2.query({1, 0}) == 11);
+    EXPECT(val(c2.query({1, 0})) == 11);
   }
   {  // tensor-matrix over two legs, blocks appended in reverse
     std::vector<T> d1{0, 1, 2, 3}, d2{4, 5, 6, 7}, d3{8, 9, 10, 11}, m{1, 2, 3, 4};
@@ -118,7 +124,7 @@ void run_cases() {
     BlockSparseTensor<T> mat(arma::uvec{2, 2});
     mat.append_block(m.data(), {0, 0}, {1, 1}, {1, 2});
     const auto c = t.contract(handle, mat, arma::umat{{0, 1}, {1, 0}});
-    EXPECT(c.query({0}) == 19 && c.query({1}) == 59 && c.query({2}) == 99);
+    EXPECT(val(c.query({0})) == 19 && val(c.query({1})) == 59 && val(c.query({2})) == 99);
     // the public metadata mirrors the reference's members
     EXPECT(c.rank == 1 && c.dimension(0) == 3);
     EXPECT(c.begin_points.n_cols == 3 && c.block_offsets(2) == 2);
@@ -134,7 +140,7 @@ void run_cases() {
     EXPECT(thrown);
     thrown = false;
     try {
-      a.query({4, 0});
+      val(a.query({4, 0}));
     } catch (const Error &) {
       thrown = true;
     }
@@ -145,6 +151,7 @@ void run_cases() {
 int main() {
   run_cases<float>();
   run_cases<double>();
+  run_cases<__half>();
   std::printf("%s (%d failed checks)\n", g_failed ? "FAIL" : "OK", g_failed);
   return g_failed;
 }

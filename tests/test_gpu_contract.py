@@ -1,7 +1,9 @@
 """Parity of the CUDA contraction path with the oracle (through the C ABI via
 the Python mirror).  Integer work (pair list, boxes, offsets) is bit-exact;
 FP64 values agree within 1e-12 of max|C| (the reference's tolerance claim),
-FP32 within 1e-5."""
+FP32 within 1e-5, half (binary16 storage, FP32 accumulation, one rounding of
+each output element) within 1e-3 against the oracle on the same rounded
+inputs."""
 import numpy as np
 import pytest
 
@@ -12,6 +14,7 @@ pytestmark = pytest.mark.gpu
 
 TOL64 = 1e-12
 TOL32 = 1e-5
+TOL16 = 1e-3
 
 
 def to_gpu(tq, dim, begin, end, data, tables=None, dtype=np.float64):
@@ -82,6 +85,26 @@ def test_small_u1_float32(tq, small):
     hA = host(c.A.dimension, c.A.begin, c.A.end, a32)
     hB = host(c.B.dimension, c.B.begin, c.B.end, b32)
     check_reference_layout(tq, A, B, hA, hB, c.pairs, np.float32, TOL32)
+
+
+def test_small_u1_float16(tq, small):
+    c = small
+    A = to_gpu(tq, c.A.dimension, c.A.begin, c.A.end, c.a_data, dtype=np.float16)
+    B = to_gpu(tq, c.B.dimension, c.B.begin, c.B.end, c.b_data, dtype=np.float16)
+    a16 = c.a_data.astype(np.float16).astype(np.float64)
+    b16 = c.b_data.astype(np.float16).astype(np.float64)
+    hA = host(c.A.dimension, c.A.begin, c.A.end, a16)
+    hB = host(c.B.dimension, c.B.begin, c.B.end, b16)
+    C = check_reference_layout(tq, A, B, hA, hB, c.pairs, np.float16, TOL16)
+    assert C.dtype == np.float16
+    # the rank-0 path (every leg contracted) in half, scaled to stay far below
+    # the binary16 maximum (65504)
+    X = to_gpu(tq, c.A.dimension, c.A.begin, c.A.end, 0.25 * c.a_data, dtype=np.float16)
+    x16 = (0.25 * c.a_data).astype(np.float16).astype(np.float64)
+    full = np.array([[0, 0], [1, 1], [2, 2], [3, 3]])
+    s = A.contract(X, full).to_number()
+    want = float(np.dot(a16, x16))
+    assert abs(float(s) - want) <= TOL16 * abs(want)
 
 
 def test_non_adjacent_free_legs(tq, small):
@@ -187,7 +210,8 @@ def test_allocation_failure_is_reported(tq, small):
 
 
 @pytest.mark.parametrize("layout", ["reference", "reduced"])
-@pytest.mark.parametrize("dtype,tol", [(np.float64, TOL64), (np.float32, TOL32)])
+@pytest.mark.parametrize("dtype,tol", [(np.float64, TOL64), (np.float32, TOL32),
+                                       (np.float16, TOL16)])
 def test_split_k_few_tiles_long_k(tq, layout, dtype, tol):
     """Few output tiles with a long fused K: the native kernel cuts each tile
     into K chunks (boundaries inside pairs) and sums the partials in chunk
@@ -199,8 +223,9 @@ def test_split_k_few_tiles_long_k(tq, layout, dtype, tol):
     A = charge_blocks([fa, cl, cl.flipped()])
     B = charge_blocks([cl.flipped(), cl, fe])
     rng = np.random.default_rng(17)
-    a = rng.standard_normal(A.n_elem)
-    b = rng.standard_normal(B.n_elem)
+    # the oracle sees the inputs rounded to the tensor's type
+    a = rng.standard_normal(A.n_elem).astype(dtype).astype(np.float64)
+    b = rng.standard_normal(B.n_elem).astype(dtype).astype(np.float64)
     pairs = np.array([[1, 0], [2, 1]])
     gA = to_gpu(tq, A.dimension, A.begin, A.end, a, dtype=dtype)
     gB = to_gpu(tq, B.dimension, B.begin, B.end, b, dtype=dtype)

@@ -126,3 +126,29 @@ def test_plan_reuse_and_unsupported(tq):
     with pytest.raises(tq.TorqueError) as ei:
         X.contract(Y, [[1, 0]], precision="ozaki")
     assert ei.value.status == 5
+
+
+def test_bounded_wait_gives_up_and_reports(tq):
+    """The failure path of the tensor-core pipeline, without a GPU fault: with a
+    1 ms wait limit and the producer held back for 50 ms before it issues
+    anything, the MMA and epilogue roles give up their waits, the kernel drains
+    and frees its tensor memory, and the check reports TQ_ERR_TIMEOUT (nothing
+    is left in flight: the producer then sees the abort flag and issues no
+    copy).  Contractions made after the reset run normally."""
+    c = workloads.small_u1()
+    A, B, hA, hB = gpu_pair(tq, c)
+    lib = tq.load()
+    lib.tq_debug_set_waits(1_000_000, 50_000_000)
+    try:
+        P = tq.ContractionPlan(A, B, c.pairs, precision="ozaki", slices=5, layout="reduced")
+    finally:
+        lib.tq_debug_set_waits(0, 0)
+    P.execute()
+    with pytest.raises(tq.TorqueError) as ei:
+        P.check()
+    assert ei.value.status == 6 and "gave up" in str(ei.value)
+    del P
+    # the library and the GPU carry on: a fresh plan (default limits) is exact
+    C = A.contract(B, c.pairs, precision="ozaki", layout="reduced")
+    N = A.contract(B, c.pairs, layout="reduced")
+    assert rel_err(C.data(), N.data()) <= 1e-10

@@ -163,3 +163,11 @@ def test_overlapping_boxes_and_partial_intervals():
     C = orc.HostBS(np.array([6, 5, 4]), ob, oe, data, offsets=off)
     want = orc.dense_contract(orc.densify(A), orc.densify(B), pairs)
     assert np.allclose(orc.densify(C), want, rtol=0, atol=1e-12)
+
+
+def test_slice_boxes_hand_case():
+    """slice restated (block_sparse.cuh:1124-1176): a 4 x 6 block cut by (2, 3)
+    gives six 2 x 2 sub-boxes, leg 0 fastest."""
+    b, e = orc.slice_boxes([[1, 0]], [[4, 5]], [2, 3])
+    assert b.tolist() == [[1, 0], [3, 0], [1, 2], [3, 2], [1, 4], [3, 4]]
+    assert e.tolist() == [[2, 1], [4, 1], [2, 3], [4, 3], [2, 5], [4, 5]]

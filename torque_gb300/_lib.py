@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "libtorque_gb300.so")
 
 TQ_OK, TQ_ERR_INVALID, TQ_ERR_CUDA, TQ_ERR_OOM, TQ_ERR_RANGE, TQ_ERR_UNSUPPORTED, \
     TQ_ERR_TIMEOUT = range(7)
-TQ_F32, TQ_F64 = 0, 1
+TQ_F32, TQ_F64, TQ_F16 = 0, 1, 2
 TQ_MEM_HOST, TQ_MEM_DEVICE = 0, 1
 PRECISIONS = {"native": 0, "fp64": 0, "ozaki": 1, "bf16x3": 2}
 LAYOUTS = {"reference": 0, "reduced": 1}
@@ -89,6 +89,7 @@ SIGNATURES = {
     "tq_last_error_string": (ctypes.c_char_p, []),
     "tq_release_cached_memory": (ST, []),
     "tq_debug_fail_alloc_after": (None, [I64]),
+    "tq_debug_set_waits": (None, [ctypes.c_uint64, ctypes.c_uint64]),
     "tq_debug_kernel_launches": (I64, []),
 }
 

@@ -14,10 +14,11 @@ from typing import Optional, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import TQ_F32, TQ_F64, TQ_MEM_DEVICE, TQ_MEM_HOST, ContractOpts, check, load
+from ._lib import TQ_F16, TQ_F32, TQ_F64, TQ_MEM_DEVICE, TQ_MEM_HOST, ContractOpts, check, load
 
-_DT = {np.dtype(np.float64): TQ_F64, np.dtype(np.float32): TQ_F32}
-_NP = {TQ_F64: np.float64, TQ_F32: np.float32}
+_DT = {np.dtype(np.float64): TQ_F64, np.dtype(np.float32): TQ_F32,
+       np.dtype(np.float16): TQ_F16}
+_NP = {TQ_F64: np.float64, TQ_F32: np.float32, TQ_F16: np.float16}
 
 
 def _i64(a) -> np.ndarray:

@@ -323,7 +323,9 @@ static tq_status native_work(const tq_plan *P, const int64_t *tiles, const int64
   TQ_CUDA(cudaMemcpyAsync(h, tot.p, 24, cudaMemcpyDeviceToHost, s));
   TQ_CUDA(cudaStreamSynchronize(s));
   if (h[1] == 0) return TQ_OK;  // nothing long enough to split
-  TQ_CHECK(W.scratch.alloc((size_t)h[2] * NT_TM * NT_TN * dtype_size(P->A->dtype), s));
+  // partial tiles are held in the accumulation type (FP32 for binary16)
+  const size_t acc_bytes = P->A->dtype == TQ_F64 ? 8 : 4;
+  TQ_CHECK(W.scratch.alloc((size_t)h[2] * NT_TM * NT_TN * acc_bytes, s));
   W.w.n_work = h[0];
   W.w.n_split = h[1];
   W.w.work_start = W.work_start.p;

@@ -37,6 +37,8 @@
 // bulk copy per operand per k-step fills a pipeline stage.
 #include <cuda_bf16.h>
 
+#include <atomic>
+
 #include "gemm.cuh"
 #include "oz_gemm.cuh"
 #include "ozaki.cuh"
@@ -333,6 +335,14 @@ int oz_stages(int s, int tile_n) {
 
 static tq_status oz_setup(int *sms);
 
+// Pipeline wait limit and producer delay of the launches built from now on
+// (tq_debug_set_waits; the defaults are 2 s and none).
+static std::atomic<uint64_t> g_wait_ns{2000000000ull}, g_delay_ns{0};
+static void debug_waits(uint64_t *wait_ns, uint64_t *delay_ns) {
+  *wait_ns = g_wait_ns.load();
+  *delay_ns = g_delay_ns.load();
+}
+
 tq_status oz_batch_build(const std::vector<OzJob> &jobs, const std::vector<OzSide> &sides,
                          cudaStream_t st, OzBatchDev &out) {
   TQ_CHECK(oz_setup(&out.sms));
@@ -385,6 +395,7 @@ tq_status oz_batch_build(const std::vector<OzJob> &jobs, const std::vector<OzSid
   L.tile_n = tile_n;
   L.nstages = oz_stages(s_max, tile_n);
   L.err = out.err.p;
+  debug_waits(&L.wait_ns, &L.delay_ns);
   TQ_CHECK(out.tiles.alloc(std::max<int64_t>(L.n_tiles, 1), st));
   L.tiles = out.tiles.p;
   if (L.n_tiles) {
@@ -454,3 +465,8 @@ tq_status oz_batch_check(const OzBatchDev &b, cudaStream_t st) {
 }
 
 }  // namespace tq
+
+extern "C" void tq_debug_set_waits(uint64_t wait_ns, uint64_t producer_delay_ns) {
+  tq::g_wait_ns.store(wait_ns ? wait_ns : 2000000000ull);
+  tq::g_delay_ns.store(producer_delay_ns);
+}

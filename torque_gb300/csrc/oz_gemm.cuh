@@ -255,6 +255,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
     // has drained those slots: the MMA warp then only waits for its stage (the
     // stage's completion implies the drain) and keeps feeding the tensor core.
     if (lane == 0) {
+      // failure-path test hook: the producer holds back before it arms any
+      // barrier or issues any copy, so the other roles' bounded waits run out
+      // (then it sees the abort flag and issues nothing)
+      if (L.delay_ns) {
+        const uint64_t t0 = global_ns();
+        while (global_ns() - t0 < L.delay_ns) __nanosleep(1000);
+      }
       OzSlotMap<NSLOT> sm;
       sm.init();
       uint32_t it = 0;
@@ -291,7 +298,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
           const uint8_t *ga = sliceA + pr.a_off + nk * s * 256 * (OZ_M / 8) * T.mt;
           const uint8_t *gb = sliceB + pr.b_off + nk * s * 256 * (N / 8) * T.nt;
           for (int64_t q = 0; q < nk; q++, it++) {
-            if (it >= (uint32_t)NS && !mbar_wait(&empty_bar[st], ph)) {
+            if (it >= (uint32_t)NS && !mbar_wait(&empty_bar[st], ph, L.wait_ns)) {
               atomicOr(L.err, 1);
               abort_flag = 1;
               break;
@@ -302,7 +309,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
               for (int a = 0; a < OZ_NACC; a++) {
                 const uint32_t p = sm.slot(a);
                 if (((fresh >> a) & 1) && sm.needs_drain(p) &&
-                    !mbar_wait(&slot_empty[p], sm.drain_parity(p)))
+                    !mbar_wait(&slot_empty[p], sm.drain_parity(p), L.wait_ns))
                   ok = false;
               }
               if (!ok) {
@@ -338,7 +345,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       // drain: every copy issued must land before the CTA may exit
       const uint32_t first = it > (uint32_t)NS ? it - NS : 0;
       for (uint32_t q = first; q < it; q++) {
-        if (!mbar_wait(&full_bar[q % NS], (q / NS) & 1)) atomicOr(L.err, 2);
+        if (!mbar_wait(&full_bar[q % NS], (q / NS) & 1, L.wait_ns)) atomicOr(L.err, 2);
       }
     }
   } else if (warp == 1) {
@@ -384,7 +391,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
           if (sidx + 1 < T.seg1) nk_next = prs[sidx + 1].nk;
           for (int64_t q = 0; q < nk; q++, it++) {
             int ok = 1;
-            if (lane == 0) ok = mbar_wait(&full_bar[st], ph);
+            if (lane == 0) ok = mbar_wait(&full_bar[st], ph, L.wait_ns);
             if (!__shfl_sync(FULL, ok, 0)) {
               if (lane == 0) {
                 atomicOr(L.err, 4);
@@ -433,7 +440,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       // every MMA issued must finish before TMEM is released
       if (elect_one()) mma_commit(&done_bar);
       __syncwarp();
-      if (lane == 0 && !mbar_wait(&done_bar, 0)) atomicOr(L.err, 32);
+      if (lane == 0 && !mbar_wait(&done_bar, 0, L.wait_ns)) atomicOr(L.err, 32);
     }
   } else {
     // ---------------- epilogue: 8 warps; warp -> TMEM lane quarter, column half
@@ -477,7 +484,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
           if (a >= n_acc || (!done && a != ev_kind)) continue;
           const uint32_t p = sm.slot(a);
           // the retirement being drained is the (par_p + 1)-th of slot p
-          if (!mbar_wait(&slot_full[p], ((sm.par >> p) & 1))) {
+          if (!mbar_wait(&slot_full[p], ((sm.par >> p) & 1), L.wait_ns)) {
             atomicOr(L.err, 16);
             abort_flag = 1;
             break;

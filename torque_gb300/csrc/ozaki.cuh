@@ -128,6 +128,8 @@ struct OzLaunch {
   int32_t s_all;           // the slice count of every job, or 0 when they differ
   int32_t *err;
   const OzTileRec *tiles;  // [n_tiles]
+  uint64_t wait_ns;        // limit of every pipeline wait (nanoseconds of wall time)
+  uint64_t delay_ns;       // producer start delay (failure-path tests only; else 0)
 };
 
 // Device copies of the job and side lists plus their prefix sums.

@@ -1,6 +1,7 @@
 // Tensor lifecycle, element access and metadata of the block-sparse tensor.
 // Mirrors torque::gpu::BlockSparseTensor (src/gpu/block_sparse.cuh:143-552,
 // 1124-1176); errors become status codes instead of exit().
+#include <cuda_fp16.h>
 #include <cstring>
 #include <atomic>
 #include <mutex>
@@ -80,7 +81,7 @@ void dev_free(void *p, cudaStream_t s) {
   if (p) cudaFreeAsync(p, s);
 }
 
-size_t dtype_size(tq_dtype t) { return t == TQ_F32 ? 4 : 8; }
+size_t dtype_size(tq_dtype t) { return t == TQ_F16 ? 2 : t == TQ_F32 ? 4 : 8; }
 
 tq_bs *new_tensor(tq_dtype dt, int32_t rank, const int64_t *dimension) {
   tq_bs *t = new tq_bs();
@@ -210,7 +211,8 @@ tq_status tq_bs_create_empty(tq_dtype dtype, int32_t rank, const int64_t *dimens
   if (!out) return fail(TQ_ERR_INVALID, "out is NULL");
   if (rank < 0 || rank > TQ_MAXR) return fail(TQ_ERR_UNSUPPORTED, "rank outside 0..12");
   if (rank && !dimension) return fail(TQ_ERR_INVALID, "dimension is NULL");
-  if (dtype != TQ_F32 && dtype != TQ_F64) return fail(TQ_ERR_INVALID, "unknown dtype");
+  if (dtype != TQ_F32 && dtype != TQ_F64 && dtype != TQ_F16)
+    return fail(TQ_ERR_INVALID, "unknown dtype");
   tq_bs *t = new_tensor(dtype, rank, dimension);
   // The reference allocates one zeroed element (block_sparse.cuh:180-187);
   // for rank 0 it is the scalar.
@@ -450,16 +452,24 @@ tq_status tq_bs_query(const tq_bs *t, const int64_t *idx, void *value) {
       double v;
       TQ_CUDA(cudaMemcpy(&v, (const double *)t->data + a, 8, cudaMemcpyDeviceToHost));
       acc += v;
-    } else {
+    } else if (t->dtype == TQ_F32) {
       float v;
       TQ_CUDA(cudaMemcpy(&v, (const float *)t->data + a, 4, cudaMemcpyDeviceToHost));
       accf += v;
+    } else {
+      __half v;
+      TQ_CUDA(cudaMemcpy(&v, (const __half *)t->data + a, 2, cudaMemcpyDeviceToHost));
+      accf += __half2float(v);
     }
   }
-  if (t->dtype == TQ_F64)
+  if (t->dtype == TQ_F64) {
     std::memcpy(value, &acc, 8);
-  else
+  } else if (t->dtype == TQ_F32) {
     std::memcpy(value, &accf, 4);
+  } else {
+    const __half h = __float2half_rn(accf);
+    std::memcpy(value, &h, 2);
+  }
   return TQ_OK;
 }
 
@@ -483,8 +493,9 @@ tq_status tq_bs_modify(tq_bs *t, const int64_t *idx, const void *value) {
       TQ_CUDA(cudaMemset((char *)t->data + element_address(t, hits[q], idx) * es, 0, es));
     return TQ_OK;
   }
-  const bool nonzero = t->dtype == TQ_F64 ? *(const double *)value != 0.0
-                                          : *(const float *)value != 0.0f;
+  const bool nonzero = t->dtype == TQ_F64   ? *(const double *)value != 0.0
+                       : t->dtype == TQ_F32 ? *(const float *)value != 0.0f
+                                            : __half2float(*(const __half *)value) != 0.0f;
   if (!nonzero) return TQ_OK;
   // a one-element block with an all-zero index table, as the reference appends
   std::vector<int64_t> zeros(t->rank, 0);

@@ -293,10 +293,13 @@ extern "C" tq_status tq_bs_hard_transpose(const tq_bs *t, const int64_t *perm, t
       TQ_CUDA(cudaGetDevice(&dev));
       TQ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
       const unsigned grid = (unsigned)std::min<int64_t>(n_tiles, 6 * (int64_t)sms);
+      // a transpose moves bits: the element size picks the kernel
       if (t->dtype == TQ_F64)
         count_launch(), transpose_kernel<double><<<grid, 256, 0, s>>>(job, n_tiles);
-      else
+      else if (t->dtype == TQ_F32)
         count_launch(), transpose_kernel<float><<<grid, 256, 0, s>>>(job, n_tiles);
+      else
+        count_launch(), transpose_kernel<unsigned short><<<grid, 256, 0, s>>>(job, n_tiles);
       TQ_CUDA(cudaGetLastError());
     }
   }
