@@ -115,8 +115,8 @@ __global__ void __launch_bounds__(256) transpose_kernel(TransposeJob job, int64_
   __shared__ int64_t base_in[PLANES_MAX], base_out[PLANES_MAX];
   const int r = job.rank;
   const int p0 = job.perm[0];
-  const T *src = (const T *)job.in.data;
-  T *dst = (T *)job.out;
+  const T *__restrict__ src = (const T *)job.in.data;
+  T *__restrict__ dst = (T *)job.out;
   const int tid = threadIdx.x;
   for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
     const int64_t b = job.tile_block[t];
@@ -135,6 +135,9 @@ __global__ void __launch_bounds__(256) transpose_kernel(TransposeJob job, int64_
     }
     const PlanePlan pp = plane_plan(d, r, p0);
     const int64_t ib0 = job.in.offsets[b], ob0 = job.out_off[b];
+    // the strides the element loops use, in registers: read through pointers
+    // they would be reloaded after every store (the stores might alias them)
+    const int64_t s0 = st[0], sp = st[p0], o0 = ost[0], op = ost[p0];
     __syncthreads();  // the previous tile is done with the shared arrays
     if (pp.mode == 2) {
       // one 32 x 32 tile of a large plane
@@ -146,12 +149,12 @@ __global__ void __launch_bounds__(256) transpose_kernel(TransposeJob job, int64_
       const int tx = tid & 31, ty = tid >> 5;
       for (int q = ty; q < TT; q += 8) {
         const uint32_t ii = i0 + tx, jj = j0 + q;
-        if (ii < d[0] && jj < d[p0]) tile[q][tx] = src[ib + ii * st[0] + jj * st[p0]];
+        if (ii < d[0] && jj < d[p0]) tile[q][tx] = src[ib + ii * s0 + jj * sp];
       }
       __syncthreads();
       for (int q = ty; q < TT; q += 8) {
         const uint32_t jj = j0 + tx, ii = i0 + q;
-        if (ii < d[0] && jj < d[p0]) dst[ob + jj * ost[p0] + ii * ost[0]] = tile[tx][q];
+        if (ii < d[0] && jj < d[p0]) dst[ob + jj * op + ii * o0] = tile[tx][q];
       }
       continue;
     }
@@ -162,7 +165,7 @@ __global__ void __launch_bounds__(256) transpose_kernel(TransposeJob job, int64_
       int64_t ib = ib0, ob = ob0;
       plane_bases(local / npc, d, st, ost, r, p0, ib, ob);
       for (uint32_t i = i0 + tid; i < d[0] && i < i0 + PLANE_MAX; i += 256)
-        dst[ob + i * ost[0]] = src[ib + i * st[0]];
+        dst[ob + i * o0] = src[ib + i * s0];
       continue;
     }
     // batched planes: bases first, one thread per plane
@@ -181,7 +184,7 @@ __global__ void __launch_bounds__(256) transpose_kernel(TransposeJob job, int64_
       const uint32_t n = nrows * d[0];
       for (uint32_t e = tid; e < n; e += 256) {
         const uint32_t pi = by_d0.div(e), i = e - pi * d[0];
-        dst[base_out[pi] + i * ost[0]] = src[base_in[pi] + i * st[0]];
+        dst[base_out[pi] + i * o0] = src[base_in[pi] + i * s0];
       }
       continue;
     }
@@ -190,12 +193,12 @@ __global__ void __launch_bounds__(256) transpose_kernel(TransposeJob job, int64_
     const SmallDiv by_pl(PL), by_d0(d0), by_dp(dp);
     for (uint32_t e = tid; e < n; e += 256) {
       const uint32_t pi = by_pl.div(e), w = e - pi * PL, j = by_d0.div(w), i = w - j * d0;
-      buf[pi * pp.P + i + j * (d0 + 1)] = src[base_in[pi] + i * st[0] + j * st[p0]];
+      buf[pi * pp.P + i + j * (d0 + 1)] = src[base_in[pi] + i * s0 + j * sp];
     }
     __syncthreads();
     for (uint32_t f = tid; f < n; f += 256) {
       const uint32_t pi = by_pl.div(f), w = f - pi * PL, i = by_dp.div(w), j = w - i * dp;
-      dst[base_out[pi] + j * ost[p0] + i * ost[0]] = buf[pi * pp.P + i + j * (d0 + 1)];
+      dst[base_out[pi] + j * op + i * o0] = buf[pi * pp.P + i + j * (d0 + 1)];
     }
   }
 }
