@@ -197,6 +197,39 @@ tq_status tq_bs_fuse_legs(const tq_bs *t, int32_t leg, int64_t n_sec_a, const in
                           int64_t n_sec_b, const int64_t *bounds_b, const int64_t *pair_offset,
                           tq_stream stream, tq_bs **out);
 
+/* Inverse of tq_bs_fuse_legs (no reference counterpart; a sweep needs it to go
+ * back from D^2 to D x D without leaving the device): leg `leg` becomes legs
+ * `leg` (dim bounds_a[n_sec_a]) and `leg`+1 (dim bounds_b[n_sec_b]), with the
+ * same sector bounds and pair offsets that fused them.  Every block must cover
+ * exactly one sector pair's range of the leg; its data are already in the split
+ * layout and are copied unchanged. */
+tq_status tq_bs_split_leg(const tq_bs *t, int32_t leg, int64_t n_sec_a, const int64_t *bounds_a,
+                          int64_t n_sec_b, const int64_t *bounds_b, const int64_t *pair_offset,
+                          tq_stream stream, tq_bs **out);
+
+/* Block lists of charge-conserving (U(1) or Z_n) tensors (no reference
+ * counterpart: Torque leaves the mapping of symmetry sectors to boxes to its
+ * caller, src/tensor/block_sparse.h:109-145).  Leg l has n_sectors[l] sectors
+ * whose charges and sizes are concatenated over the legs (leg 0 first), laid out
+ * as contiguous coordinate ranges in the given order, and a direction
+ * directions[l] = +1 (incoming) or -1 (outgoing).  A block exists for every
+ * sector tuple with sum(direction * charge) == total (mod modulus for Z_n;
+ * modulus 0 = U(1)); blocks are listed in column-major order of the sector
+ * indices (leg 0 fastest).  *n_blocks receives the count; when cap >= it,
+ * begin_points / end_points (rank x n_blocks, as tq_bs_create takes them) are
+ * filled.  Call once with cap = 0 to size them. */
+tq_status tq_charge_blocks(int32_t rank, const int64_t *n_sectors, const int64_t *charges,
+                           const int64_t *sizes, const int32_t *directions, int64_t total,
+                           int64_t modulus, int64_t cap, int64_t *n_blocks,
+                           int64_t *begin_points, int64_t *end_points);
+/* A tensor over that block list, its data in block order (each block
+ * column-major) from host or device memory, or all zeros when data is NULL. */
+tq_status tq_bs_create_charges(tq_dtype dtype, int32_t rank, const int64_t *n_sectors,
+                               const int64_t *charges, const int64_t *sizes,
+                               const int32_t *directions, int64_t total, int64_t modulus,
+                               const void *data, tq_memkind kind, tq_stream stream,
+                               tq_bs **out);
+
 /* slice (block_sparse.cuh:1124-1176): split every block into prod(divisor)
  * boxes without moving data, as the reference does. */
 tq_status tq_bs_slice(const tq_bs *t, const int64_t *divisor, tq_stream stream,

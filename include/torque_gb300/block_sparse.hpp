@@ -2,7 +2,7 @@
 //
 // Source-compatible with the reference class (src/gpu/block_sparse.cuh:143-1181):
 // the same constructors, public metadata members, element access, contract,
-// hard_transpose and slice, with T in {float, double}.  Differences:
+// hard_transpose and slice, with T in {float, double, half}.  Differences:
 //   * contract() takes any handle type in the first position and ignores it (no
 //     cuBLAS is used); an overload without a handle is added;
 //   * API misuse throws Error (as the reference does); CUDA failures throw
@@ -237,6 +237,51 @@ class BlockSparseTensor {
     tq_bs *out = nullptr;
     detail::check(tq_bs_fuse_legs(h_, (int32_t)leg, (int64_t)ba.size() - 1, ba.data(),
                                   (int64_t)bb.size() - 1, bb.data(), off.data(), nullptr, &out));
+    return BlockSparseTensor(out);
+  }
+
+  // Inverse of fuse_legs (an extension): leg `leg` split back into two legs,
+  // with the bounds and pair offsets that fused them.  See tq_bs_split_leg.
+  BlockSparseTensor split_leg(arma::uword leg, const arma::uvec &bounds_a,
+                              const arma::uvec &bounds_b, const arma::umat &pair_offset) const {
+    if (leg >= rank) throw Error("leg to split out of range");
+    if (pair_offset.n_rows + 1 != bounds_a.n_elem || pair_offset.n_cols + 1 != bounds_b.n_elem)
+      throw Error("pair_offset must be (sectors of a) x (sectors of b)");
+    const auto ba = detail::flat(bounds_a), bb = detail::flat(bounds_b),
+               off = detail::flat(pair_offset);
+    tq_bs *out = nullptr;
+    detail::check(tq_bs_split_leg(h_, (int32_t)leg, (int64_t)ba.size() - 1, ba.data(),
+                                  (int64_t)bb.size() - 1, bb.data(), off.data(), nullptr, &out));
+    return BlockSparseTensor(out);
+  }
+
+  // A charge-conserving tensor (an extension): leg l has the sectors
+  // charges[l] / sizes[l] laid out in order and direction directions(l) (+1 in,
+  // -1 out); blocks for every sector tuple with sum(direction * charge) ==
+  // total (mod modulus for Z_n, 0 = U(1)), leg 0 fastest; data in block order,
+  // or zeros when src is NULL.  See tq_bs_create_charges.
+  static BlockSparseTensor from_charges(const std::vector<arma::Col<long long>> &charges,
+                                        const std::vector<arma::uvec> &sizes,
+                                        const std::vector<int> &directions, const T *src,
+                                        long long total = 0, long long modulus = 0,
+                                        cudaMemcpyKind kind = cudaMemcpyHostToDevice) {
+    if (charges.size() != sizes.size() || charges.size() != directions.size())
+      throw Error("one charge list, size list and direction per leg");
+    std::vector<int64_t> ns, q, sz;
+    std::vector<int32_t> dir;
+    for (size_t l = 0; l < charges.size(); l++) {
+      if (charges[l].n_elem != sizes[l].n_elem) throw Error("charges and sizes must pair up");
+      ns.push_back((int64_t)charges[l].n_elem);
+      for (arma::uword s = 0; s < charges[l].n_elem; s++) {
+        q.push_back((int64_t)charges[l](s));
+        sz.push_back((int64_t)sizes[l](s));
+      }
+      dir.push_back(directions[l]);
+    }
+    tq_bs *out = nullptr;
+    detail::check(tq_bs_create_charges(detail::dtype<T>(), (int32_t)charges.size(), ns.data(),
+                                       q.data(), sz.data(), dir.data(), total, modulus, src,
+                                       detail::kind_of(kind), nullptr, &out));
     return BlockSparseTensor(out);
   }
 

@@ -129,6 +129,17 @@ void run_cases() {
     EXPECT(c.rank == 1 && c.dimension(0) == 3);
     EXPECT(c.begin_points.n_cols == 3 && c.block_offsets(2) == 2);
   }
+  {  // charge-conserving construction (an extension): U(1) legs q in {0, 1}
+     // sized {1, 2}, legs 0 in and 1 out -> blocks (0,0) and (1,1)
+    std::vector<arma::Col<long long>> q = {arma::Col<long long>{0, 1},
+                                           arma::Col<long long>{0, 1}};
+    std::vector<arma::uvec> sz = {arma::uvec{1, 2}, arma::uvec{1, 2}};
+    std::vector<T> d = {7, 1, 2, 3, 4};
+    const auto c = BlockSparseTensor<T>::from_charges(q, sz, {1, -1}, d.data());
+    EXPECT(c.begin_points.n_cols == 2 && c.dimension(0) == 3);
+    EXPECT(val(c.query({0, 0})) == 7 && val(c.query({1, 2})) == 3);
+    EXPECT(val(c.query({0, 1})) == 0);
+  }
   {  // misuse throws Error like the reference
     BlockSparseTensor<T> a(arma::uvec{4, 3}), b(arma::uvec{5, 3});
     bool thrown = false;

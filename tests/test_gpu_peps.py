@@ -73,3 +73,42 @@ def test_fuse_legs_matches_dense_reshape(tq):
     with pytest.raises(tq.TorqueError) as ei:
         P.fuse_legs(0, [0, 3, 7], [0, 2, 5], [[0, 6], [15, 20]])  # ranges overlap
     assert ei.value.status == 1
+
+
+@pytest.mark.parametrize("modulus", [None, 2])
+def test_split_undoes_fuse_and_charge_construction(tq, modulus):
+    """A charge-conserving tensor made through the C ABI (tq_bs_create_charges)
+    has the Python constructor's block list; fusing two of its legs by charge
+    and splitting them again (tq_bs_split_leg) gives back the same blocks,
+    strides, offsets and data, bit for bit, without leaving the device."""
+    from torque_gb300.sectors import Leg, charge_blocks
+    la = Leg([-1, 0, 1], [2, 3, 2], +1)
+    lb = Leg([0, 1], [2, 3], +1)
+    lc = Leg([-1, 0, 1, 2], [1, 2, 2, 1], -1)
+    ld = Leg([0, 1], [3, 1], -1)
+    legs = [la, lb, lc, ld]
+    bl = charge_blocks(legs, modulus=modulus)
+    rng = np.random.default_rng(11)
+    data = rng.standard_normal(bl.n_elem)
+    T = tq.BlockSparseTensor.from_charges(legs, data, modulus=modulus)
+    dim, b, e, t, o = T.metadata()
+    assert np.array_equal(b.T, bl.begin) and np.array_equal(e.T, bl.end)
+    assert np.array_equal(T.data(), data)
+    for leg, (x, y) in ((0, (la, lb)), (1, (lb, lc)), (2, (lc, ld))):
+        F, fused = T.fuse_sectors(leg, x, y, modulus)
+        assert F.rank == 3
+        S = F.split_sectors(leg, x, y, modulus)
+        d2, b2, e2, t2, o2 = S.metadata()
+        assert np.array_equal(d2, dim) and np.array_equal(b2, b) and np.array_equal(e2, e)
+        assert np.array_equal(t2, t) and np.array_equal(o2, o)
+        assert np.array_equal(S.data(), data)
+    Z = tq.BlockSparseTensor.from_charges(legs, None, modulus=modulus)
+    assert Z.n_blocks == bl.n_blocks and not np.any(Z.data())
+
+
+def test_split_rejects_blocks_across_pairs(tq):
+    """A block covering two sector pairs of the leg cannot be split."""
+    T = tq.BlockSparseTensor([6, 2], np.ones(12), [[0], [0]], [[5], [1]])
+    with pytest.raises(tq.TorqueError) as ei:
+        T.split_leg(0, [0, 1, 2], [0, 3], [[0], [3]])
+    assert "exactly one sector pair" in str(ei.value)

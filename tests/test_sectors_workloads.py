@@ -2,6 +2,7 @@
 brute-force one, charge-ordered fusion tiles the fused leg, and the seeded
 workload generators are deterministic and respect their caps."""
 import numpy as np
+import pytest
 
 from torque_gb300 import sectors as S
 from torque_gb300 import workloads as W
@@ -54,3 +55,17 @@ def test_random_contractions_deterministic_and_capped():
         assert 3 <= x.A.begin.shape[1] <= 6 and 1 <= x.pairs.shape[0] <= 3
         z = W.from_spec(x.spec())
         assert np.array_equal(z.B.end, x.B.end)
+
+
+@pytest.mark.parametrize("modulus", [None, 2, 3])
+def test_charge_blocks_c_abi_matches_python(modulus):
+    """tq_charge_blocks (C ABI, host code) lists the same blocks in the same
+    order (leg 0 fastest) as the Python constructor, for U(1) and Z_n."""
+    from torque_gb300 import block_sparse
+    from torque_gb300.sectors import Leg, charge_blocks
+    legs = [Leg([-1, 0, 2], [2, 3, 1], +1), Leg([0, 1], [4, 2], +1),
+            Leg([-2, 0, 1, 3], [1, 2, 2, 1], -1), Leg([1, 0], [3, 3], -1)]
+    for total in (0, 1):
+        want = charge_blocks(legs, total=total, modulus=modulus)
+        b, e = block_sparse.charge_block_list(legs, total=total, modulus=modulus)
+        assert np.array_equal(b, want.begin) and np.array_equal(e, want.end)

@@ -280,6 +280,42 @@ class BlockSparseTensor:
         bb = np.concatenate([[0], np.cumsum(leg_b.sizes)])
         return self.fuse_legs(leg, ba, bb, off, stream), fused
 
+    def split_leg(self, leg: int, bounds_a, bounds_b, pair_offset, stream=None):
+        """Inverse of fuse_legs (tq_bs_split_leg): leg `leg` back into two legs,
+        with the sector bounds and pair offsets that fused them."""
+        ba, bb = _i64(bounds_a), _i64(bounds_b)
+        off = _i64(np.asarray(pair_offset).reshape(ba.size - 1, bb.size - 1).ravel(order="F"))
+        h = ctypes.c_void_p()
+        check(load().tq_bs_split_leg(self._h, int(leg), ba.size - 1, _p64(ba), bb.size - 1,
+                                     _p64(bb), _p64(off), _stream(stream), ctypes.byref(h)))
+        return BlockSparseTensor(_handle=h)
+
+    def split_sectors(self, leg: int, leg_a, leg_b, modulus=None, stream=None):
+        """Inverse of fuse_sectors: the charge-ordered fused leg `leg` back into
+        legs carrying sectors leg_a, leg_b (sectors.Leg)."""
+        from .sectors import fuse_sector_order
+        fused, off = fuse_sector_order(leg_a, leg_b, modulus)
+        ba = np.concatenate([[0], np.cumsum(leg_a.sizes)])
+        bb = np.concatenate([[0], np.cumsum(leg_b.sizes)])
+        return self.split_leg(leg, ba, bb, off, stream)
+
+    @classmethod
+    def from_charges(cls, legs, source_data=None, total=0, modulus=None, dtype=np.float64,
+                     stream=None) -> "BlockSparseTensor":
+        """A charge-conserving tensor over sectors.Leg legs (tq_bs_create_charges):
+        one block per sector tuple with sum(direction * charge) == total (mod
+        modulus), leg 0 fastest; data in block order, or zeros."""
+        ns, q, sz, d = charge_args(legs)
+        h = ctypes.c_void_p()
+        data, kind = (None, TQ_MEM_HOST) if source_data is None else \
+            cls._data_arg(source_data, dtype)
+        check(load().tq_bs_create_charges(_DT[np.dtype(dtype)], len(legs), _p64(ns), _p64(q),
+                                          _p64(sz), d.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                          int(total), int(modulus or 0),
+                                          None if data is None else cls._ptr(data), kind,
+                                          _stream(stream), ctypes.byref(h)))
+        return cls(_handle=h)
+
     def slice(self, divisor, stream=None) -> "BlockSparseTensor":
         d = _i64(divisor)
         h = ctypes.c_void_p()
@@ -290,6 +326,31 @@ class BlockSparseTensor:
         h = ctypes.c_void_p()
         check(load().tq_bs_clone(self._h, _stream(stream), ctypes.byref(h)))
         return BlockSparseTensor(_handle=h)
+
+
+def charge_args(legs):
+    """(sectors per leg, charges, sizes, directions) arrays of tq_charge_blocks."""
+    ns = _i64([len(l.charges) for l in legs])
+    q = _i64([c for l in legs for c in l.charges])
+    sz = _i64([x for l in legs for x in l.sizes])
+    d = np.ascontiguousarray([int(l.direction) for l in legs], dtype=np.int32)
+    return ns, q, sz, d
+
+
+def charge_block_list(legs, total=0, modulus=None):
+    """The block list tq_charge_blocks makes: (begin, end) as n_blocks x rank."""
+    ns, q, sz, d = charge_args(legs)
+    n = ctypes.c_int64()
+    dp = d.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    lib = load()
+    check(lib.tq_charge_blocks(len(legs), _p64(ns), _p64(q), _p64(sz), dp, int(total),
+                               int(modulus or 0), 0, ctypes.byref(n), None, None))
+    r = len(legs)
+    b = np.zeros(max(n.value, 1) * r, np.int64)
+    e = np.zeros_like(b)
+    check(lib.tq_charge_blocks(r, _p64(ns), _p64(q), _p64(sz), dp, int(total), int(modulus or 0),
+                               n.value, ctypes.byref(n), _p64(b), _p64(e)))
+    return b[:n.value * r].reshape(-1, r), e[:n.value * r].reshape(-1, r)
 
 
 def contract_blocks(A: "BlockSparseTensor", B: "BlockSparseTensor", contracting_indices,
