@@ -57,6 +57,7 @@ def parse():
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--no-hbm", action="store_true")
     p.add_argument("--no-costmodel", action="store_true")
+    p.add_argument("--no-sparse", action="store_true")
     return p.parse_args()
 
 
@@ -509,6 +510,8 @@ def run_ours(args):
             line["batched_sweep"] = sweep(tq)
         if not args.no_peps:
             line["peps_norm"] = peps_norm(tq)
+        if not args.no_sparse:
+            line["sparse_join"] = sparse_join(tq)
         if not args.no_costmodel:
             line["cost_model"] = cost_model(tq)
         print(json.dumps(line))
@@ -691,6 +694,52 @@ def sweep(tq, n=256, forms=(("native", 0), ("ozaki", 5), ("bf16x3", 3)), replays
         del batch, p1, p2
     res["sequential_fp64_tflops"] = res["useful_flop"] / t_seq / 1e12
     return res
+
+
+def sparse_join(tq, seed=29):
+    """Element-sparse contraction (the reference's SparseTensor path): two
+    random sparse tensors A[i,k,l] (4096 x 64 x 64) and B[k,l,j] (64 x 64 x
+    4096), 1 % filled with N(0,1) entries (seed 29), contracted over (k,l).
+    The sort-join (tq_bs_contract_elements) against the same contraction over
+    one-element blocks through the block matcher (all nnz_A x nnz_B interval
+    tests), both from the same device tensors, CUDA events, best of 3."""
+    import torch
+    from torque_gb300 import block_sparse as bs
+    rng = np.random.default_rng(seed)
+    da, db = (4096, 64, 64), (64, 64, 4096)
+    na = int(0.01 * np.prod(da))
+    nb = int(0.01 * np.prod(db))
+    ia = np.sort(rng.choice(int(np.prod(da)), na, replace=False))
+    ib = np.sort(rng.choice(int(np.prod(db)), nb, replace=False))
+    pa = np.stack(np.unravel_index(ia, da, order="F"), 1)
+    pb = np.stack(np.unravel_index(ib, db, order="F"), 1)
+    A = tq.BlockSparseTensor(da, rng.standard_normal(na), pa.T, pa.T)
+    B = tq.BlockSparseTensor(db, rng.standard_normal(nb), pb.T, pb.T)
+    pairs = [[1, 0], [2, 1]]
+
+    def timed(fn):
+        fn()
+        best = None
+        for _ in range(3):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            C = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        return best, C
+    t_join, S = timed(lambda: bs.contract_elements(A, B, pairs))
+    t_all, R = timed(lambda: A.contract(B, pairs, layout="reduced"))
+    x = _ptr_tensor(S.device_ptr(), S.n_elem)
+    y = _ptr_tensor(R.device_ptr(), R.n_elem)
+    diff = float(torch.max(torch.abs(x - y)) / torch.max(torch.abs(y))) \
+        if S.n_elem == R.n_elem else None
+    return {"nnz_a": na, "nnz_b": nb, "outputs": S.n_blocks,
+            "sort_join_ms": t_join, "all_pairs_ms": t_all, "speedup": t_all / t_join,
+            "max_rel_diff": diff,
+            "timing": "CUDA events around the whole call (symbolic and numeric), best of 3"}
 
 
 def peps_norm(tq):

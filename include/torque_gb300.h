@@ -180,6 +180,21 @@ tq_status tq_contract_blocks(const tq_bs *A, const tq_bs *B, int32_t n_legs,
                              int64_t *block_offsets, int64_t *pair_a, int64_t *pair_b,
                              tq_stream stream);
 
+/* The element-sparse contract of the reference's SparseTensor
+ * (src/gpu/sparse.cuh:270-375) for tensors whose blocks each hold one element:
+ * C[free A legs, free B legs] = sum over matching contracted indices of A B.
+ * Matches are found by sorting both operands by their contracted index and
+ * joining equal runs (O(nnz log nnz + products)), where the reference forms
+ * all nnz_A x nnz_B products.  The result has one one-element block per
+ * distinct output element, in column-major order of its coordinates (A's free
+ * legs, then B's), every product summed; unlike the reference, the first
+ * output element is kept (sparse.cuh:370-371 drops it).  Products are formed
+ * in FP64 and each sum is rounded to the element type once.  At least one leg
+ * must stay free (a full contraction to a scalar is tq_bs_contract's). */
+tq_status tq_bs_contract_elements(const tq_bs *A, const tq_bs *B, int32_t n_legs,
+                                  const int64_t *a_legs, const int64_t *b_legs,
+                                  tq_stream stream, tq_bs **out);
+
 /* hard_transpose (block_sparse.cuh:1031-1122): permute the legs of every block;
  * new leg l is old leg perm[l]. */
 tq_status tq_bs_hard_transpose(const tq_bs *t, const int64_t *perm, tq_stream stream,

@@ -111,13 +111,21 @@ class SparseTensor {
                         const arma::umat &contracting_indices) const {
     return contract(tensor, contracting_indices);
   }
+  // Matching nonzeros are found by sorting both operands by their contracted
+  // index (tq_bs_contract_elements), not by testing every pair; a contraction
+  // over every leg (a scalar) takes the block path.
   SparseTensor contract(const SparseTensor &tensor, const arma::umat &contracting_indices) const {
     std::vector<int64_t> al, bl;
     detail::contract_legs(contracting_indices, al, bl);
-    const tq_contract_opts o = {TQ_PREC_NATIVE, TQ_LAYOUT_REDUCED, 0, 0, 0, 0};
     tq_bs *out = nullptr;
-    detail::check(tq_bs_contract(h_, tensor.h_, (int32_t)al.size(), al.data(), bl.data(), &o,
-                                 nullptr, &out));
+    if (rank + tensor.rank > 2 * al.size()) {
+      detail::check(tq_bs_contract_elements(h_, tensor.h_, (int32_t)al.size(), al.data(),
+                                            bl.data(), nullptr, &out));
+    } else {
+      const tq_contract_opts o = {TQ_PREC_NATIVE, TQ_LAYOUT_REDUCED, 0, 0, 0, 0};
+      detail::check(tq_bs_contract(h_, tensor.h_, (int32_t)al.size(), al.data(), bl.data(), &o,
+                                   nullptr, &out));
+    }
     return SparseTensor(out);
   }
 

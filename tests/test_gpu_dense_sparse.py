@@ -154,3 +154,40 @@ def test_sparse_random_against_dense(tq):
     got = got.reshape(want.shape, order="F")
     assert np.max(np.abs(got - want)) <= 1e-12 * max(np.max(np.abs(want)), 1e-300)
     assert np.all(np.diff(C.indices) > 0)
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.float64, 1e-12), (np.float32, 1e-5),
+                                       (np.float16, 1e-3)])
+def test_sort_join_matches_block_matcher(tq, dtype, tol):
+    """The sort-join element contraction (tq_bs_contract_elements) against the
+    block path over the same one-element blocks (all-pairs interval matching,
+    reduced layout): the same output elements in the same order, values within
+    the type's tolerance; repeated nonzeros (duplicate coordinates) are summed."""
+    from torque_gb300 import block_sparse as bs
+    rng = np.random.default_rng(23)
+    da, db = (40, 16, 12), (16, 12, 30)
+    na, nb = 3000, 2500
+    pa = np.stack([rng.integers(0, d, na) for d in da], 1)
+    pb = np.stack([rng.integers(0, d, nb) for d in db], 1)
+    pa[1] = pa[0]  # a duplicate coordinate
+    va = rng.standard_normal(na).astype(dtype)
+    vb = rng.standard_normal(nb).astype(dtype)
+    A = tq.BlockSparseTensor(da, va, pa.T, pa.T, dtype=dtype)
+    B = tq.BlockSparseTensor(db, vb, pb.T, pb.T, dtype=dtype)
+    pairs = [[1, 0], [2, 1]]
+    S = bs.contract_elements(A, B, pairs)
+    R = A.contract(B, pairs, layout="reduced")
+    ds, sb, se, st, so = S.metadata()
+    dr, rb, re_, rt, ro = R.metadata()
+    assert np.array_equal(sb, rb) and np.array_equal(se, re_) and np.array_equal(so, ro)
+    x, y = S.data().astype(np.float64), R.data().astype(np.float64)
+    assert np.max(np.abs(x - y)) <= tol * np.max(np.abs(y))
+    # against numpy on the dense arrays (duplicates summed)
+    a = np.zeros(da)
+    np.add.at(a, tuple(pa.T), va.astype(np.float64))
+    b = np.zeros(db)
+    np.add.at(b, tuple(pb.T), vb.astype(np.float64))
+    want = np.tensordot(a, b, axes=([1, 2], [0, 1]))
+    got = want * 0
+    got[tuple(sb)] = x
+    assert np.max(np.abs(got - want)) <= 10 * tol * np.max(np.abs(want))

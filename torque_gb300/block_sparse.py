@@ -328,6 +328,18 @@ class BlockSparseTensor:
         return BlockSparseTensor(_handle=h)
 
 
+def contract_elements(A: "BlockSparseTensor", B: "BlockSparseTensor", contracting_indices,
+                      stream=None) -> "BlockSparseTensor":
+    """Element-sparse contraction (one-element blocks) by sort-join
+    (tq_bs_contract_elements): one-element result blocks in output-index order."""
+    ci = np.asarray(contracting_indices, dtype=np.int64).reshape(-1, 2)
+    al, bl = _i64(ci[:, 0]), _i64(ci[:, 1])
+    h = ctypes.c_void_p()
+    check(load().tq_bs_contract_elements(A._h, B._h, ci.shape[0], _p64(al), _p64(bl),
+                                         _stream(stream), ctypes.byref(h)))
+    return BlockSparseTensor(_handle=h)
+
+
 def charge_args(legs):
     """(sectors per leg, charges, sizes, directions) arrays of tq_charge_blocks."""
     ns = _i64([len(l.charges) for l in legs])

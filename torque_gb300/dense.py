@@ -153,8 +153,14 @@ class SparseTensor:
         return self._bs.to_number()
 
     def contract(self, tensor: "SparseTensor", contracting_indices) -> "SparseTensor":
-        return SparseTensor(_bs=self._bs.contract(tensor._bs, contracting_indices,
-                                                  layout="reduced"))
+        """Matching nonzeros found by sorting both operands by their contracted
+        index (tq_bs_contract_elements); a contraction to a scalar takes the
+        block path."""
+        ci = np.asarray(contracting_indices, dtype=np.int64).reshape(-1, 2)
+        if self.rank + tensor.rank > 2 * ci.shape[0]:
+            from .block_sparse import contract_elements
+            return SparseTensor(_bs=contract_elements(self._bs, tensor._bs, ci))
+        return SparseTensor(_bs=self._bs.contract(tensor._bs, ci, layout="reduced"))
 
     def soft_transpose(self, permutation):
         p = _i64(permutation)
