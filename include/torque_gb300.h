@@ -245,6 +245,23 @@ tq_status tq_bs_create_charges(tq_dtype dtype, int32_t rank, const int64_t *n_se
                                const void *data, tq_memkind kind, tq_stream stream,
                                tq_bs **out);
 
+/* Block-level truncated SVD for PEPS / MPS sweeps (no reference counterpart:
+ * the reference has only a cuSOLVER QR example that nothing calls,
+ * test/cusolver_playground.cpp:7).  Legs row_legs (in that order) against the
+ * others (ascending): the tensor is block diagonal over classes of row and
+ * column boxes linked by blocks (one per charge sector for a symmetric
+ * tensor); each class matrix is decomposed in FP64 by one-sided Jacobi
+ * rotations on the device; the singular values of all classes are ranked
+ * together and at most max_keep of them (all when max_keep <= 0) above
+ * cutoff * the largest are kept (zeros never).  Returns U[row legs..., bond],
+ * S[bond] and V[bond, column legs...] over a new bond leg with one sector per
+ * class that keeps values (values descending within a sector), so that T is
+ * approximated by sum_k U[..., k] S[k] V[k, ...].  float64 tensors whose
+ * blocks are sector boxes (intervals of a leg equal or disjoint). */
+tq_status tq_bs_svd(const tq_bs *t, int32_t n_row_legs, const int64_t *row_legs,
+                    int64_t max_keep, double cutoff, tq_stream stream, tq_bs **U, tq_bs **S,
+                    tq_bs **V);
+
 /* slice (block_sparse.cuh:1124-1176): split every block into prod(divisor)
  * boxes without moving data, as the reference does. */
 tq_status tq_bs_slice(const tq_bs *t, const int64_t *divisor, tq_stream stream,

@@ -316,6 +316,18 @@ class BlockSparseTensor:
                                           _stream(stream), ctypes.byref(h)))
         return cls(_handle=h)
 
+    def svd(self, row_legs, max_keep: int = 0, cutoff: float = 0.0, stream=None):
+        """Block-level truncated SVD (tq_bs_svd): row_legs against the other
+        legs; returns (U[row legs..., bond], S[bond], V[bond, other legs...])
+        keeping at most max_keep values (0: all) above cutoff * the largest."""
+        rl = _i64(row_legs)
+        u, sv, v = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        check(load().tq_bs_svd(self._h, rl.size, _p64(rl), int(max_keep), float(cutoff),
+                               _stream(stream), ctypes.byref(u), ctypes.byref(sv),
+                               ctypes.byref(v)))
+        return (BlockSparseTensor(_handle=u), BlockSparseTensor(_handle=sv),
+                BlockSparseTensor(_handle=v))
+
     def slice(self, divisor, stream=None) -> "BlockSparseTensor":
         d = _i64(divisor)
         h = ctypes.c_void_p()
