@@ -462,14 +462,17 @@ def run_ours(args):
         roof["kernel"] = "oz_gemm_kernel" if args.precision != "native" else "gemm_native_kernel"
         roof["kernel_ms"] = g_ms
         roof["prepare_ms"] = statistics.mean(prep_ms)
-        tr = os.path.join(ROOT, "profiles", "traffic.json")
+        # DRAM bytes of one launch from an ncu capture of the same workload
+        tr = os.path.join(ROOT, "profiles", "dram_traffic_oz_gemm_kernel_uneven_u1.json")
         roof["traffic"] = None
         if os.path.exists(tr):
             with open(tr) as f:
                 td = json.load(f)
             ent = td.get(roof["kernel"])
-            if ent and ent.get("peak") == args.peak and ent.get("slices") in (None, args.slices):
+            if ent and ent.get("peak") == args.peak and ent.get("qmax") == args.qmax and \
+                    ent.get("slices") in (None, args.slices) and args.precision == "ozaki":
                 roof["traffic"] = ent["bytes_per_launch"]
+                roof["traffic_source"] = "profiles/" + ent["source"]
         line["roofline"] = roof
 
         if not args.no_e2e:
