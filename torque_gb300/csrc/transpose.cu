@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(256, 4) transpose_kernel(TransposeJob job, int
 // the unstaged paths (32 x 32 tiles, straight copies) in their turn.
 constexpr int ACAP = 3072;    // elements per stage
 constexpr int APLANES = 128;  // planes per tile
-constexpr int AT = 256;       // threads per CTA
+constexpr int AT = 128;       // threads per CTA (fewer threads amortise each tile's set-up over more elements)
 
 // Everything a tile needs about its block, computed once per call by
 // describe_kernel; a tile reads it with six 16-byte loads.
@@ -487,6 +487,20 @@ __global__ void __launch_bounds__(AT, 4)
   T *__restrict__ dst = (T *)job.out;
   const uint32_t tid = threadIdx.x;
 
+  // plane output bases owed to the stage last prefetched: a contiguous tile
+  // needs them only when it is written out, so they are computed after the
+  // current tile's stores, off the path to the barrier
+  int64_t owed_b = -1, owed_ob0 = 0;
+  uint32_t owed_row0 = 0, owed_nrows = 0;
+  auto pay_bases = [&](int s) {
+    if (owed_b >= 0 && tid < owed_nrows) {
+      int64_t ib = 0, ob = owed_ob0;
+      plane_bases_of(job, owed_b, owed_row0 + tid, ib, ob);
+      bout[s][tid] = ob;
+    }
+    owed_b = -1;
+  };
+
   // start the copies of tile t into stage s (one commit group per call)
   auto prefetch = [&](int64_t t, int s) {
     const int64_t b = job.tile_block[t];
@@ -499,7 +513,12 @@ __global__ void __launch_bounds__(AT, 4)
       const uint32_t PL = D.PL, d0 = D.d0, n = nrows * PL;  // n <= ACAP
       const T *s0p = src + D.ib0 + (int64_t)row0 * PL;
       const uint32_t sh = contig && mode == 0 ? (uint32_t)(((uintptr_t)s0p & 15u) / sizeof(T)) : 0u;
-      if (tid < nrows) {
+      if (contig) {
+        owed_b = b;
+        owed_ob0 = D.ob0;
+        owed_row0 = row0;
+        owed_nrows = nrows;
+      } else if (tid < nrows) {
         int64_t ib = D.ib0, ob = D.ob0;
         plane_bases_of(job, b, row0 + tid, ib, ob);
         bin[tid] = ib;
@@ -561,6 +580,7 @@ __global__ void __launch_bounds__(AT, 4)
   if (t >= n_tiles) return;
   int k = 0;
   prefetch(t, 0);
+  pay_bases(0);
   for (; t < n_tiles; t += gridDim.x) {
     const int64_t tn = t + gridDim.x;
     // stage k^1 was last read by the previous tile's stores, which ended at
@@ -614,7 +634,8 @@ __global__ void __launch_bounds__(AT, 4)
         __stcs(dst + bout[k][pi] + j + i * I.o0, buf[k][pi * I.P + i + j * (I.d0 + 1)]);
       }
     }
-    __syncthreads();  // stage k and its bases are free again
+    pay_bases(k ^ 1);  // bases of the tile now in flight
+    __syncthreads();   // stage k is free again; the owed bases are visible
     k ^= 1;
   }
 }
