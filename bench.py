@@ -849,44 +849,65 @@ def cost_model(tq, n_live=200):
     return out
 
 
+class _DeviceView:
+    """A raw device pointer seen by torch (no copy): __cuda_array_interface__."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False),
+                                         "version": 3}
+
+
 def e2e(tq, c, ah, bh, kw, steps, ch=None):
-    """The same contraction through the C ABI from pinned host buffers: H2D of
-    both inputs, contraction, D2H of the whole result (into ch), every step."""
-    import ctypes
+    """The same contraction through the C ABI from pinned host buffers, every
+    step: both inputs copied from host memory into the operand tensors
+    (tq_bs_set_data; the tensors are created from the same host buffers in
+    the first, untimed pass), the plan, and tq_plan_execute_to into the pinned
+    host result ch — the GEMM's epilogue writes the result over the host link
+    while it runs, so no device-to-host copy follows it.  The last step's host
+    result is compared bit for bit with the same plan's device result."""
     import torch
-    from torque_gb300 import _lib
     an, bn = ah.numpy(), bh.numpy()
     times, phases = [], []
+    same = None
+    A = B = None
     for s in range(steps + 1):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        A = tq.BlockSparseTensor(c.A.dimension, an, c.A.begin.T, c.A.end.T)
-        B = tq.BlockSparseTensor(c.B.dimension, bn, c.B.begin.T, c.B.end.T)
-        t1 = time.perf_counter()  # creation from host memory returns after its copy
+        if A is None:
+            A = tq.BlockSparseTensor(c.A.dimension, an, c.A.begin.T, c.A.end.T)
+            B = tq.BlockSparseTensor(c.B.dimension, bn, c.B.begin.T, c.B.end.T)
+        else:
+            A.set_data(an)
+            B.set_data(bn)
+        t1 = time.perf_counter()  # the host-to-device copies are complete
         P = tq.ContractionPlan(A, B, c.pairs, **kw)
-        P.execute()
-        P.check()
-        C = P.result
         if ch is None:
-            ch = torch.empty(C.n_elem, dtype=torch.float64, pin_memory=True)
+            ch = torch.empty(P.result.n_elem, dtype=torch.float64, pin_memory=True)
         t2 = time.perf_counter()
-        _lib.check(_lib.load().tq_bs_copy_data(C.handle, ctypes.c_void_p(ch.data_ptr()),
-                                               _lib.TQ_MEM_HOST, None))
+        P.execute_to(ch)  # returns with the result in ch
+        P.check()
         t3 = time.perf_counter()
         dt = t3 - t
         fl = P.flops
-        del P, C, A, B
+        if s == steps:
+            P.execute()
+            dev = torch.as_tensor(_DeviceView(P.result.device_ptr(), P.result.n_elem),
+                                  device="cuda")
+            same = bool(torch.equal(dev, ch[:P.result.n_elem].to("cuda", non_blocking=False)))
+        del P
         if s > 0:  # the first pass pins pages and warms the allocator
             times.append(dt)
             phases.append((t1 - t, t2 - t1, t3 - t2))
     dt = statistics.median(times)
     ph = phases[times.index(dt)] if dt in times else phases[0]
     return {"value": fl / dt / 1e12, "unit": "TFLOP/s", "ms_per_step": dt * 1e3,
-            "phases_ms": {"h2d_create": ph[0] * 1e3, "plan_execute": ph[1] * 1e3,
-                          "d2h": ph[2] * 1e3},
+            "phases_ms": {"h2d": ph[0] * 1e3, "plan": ph[1] * 1e3,
+                          "execute_to_host": ph[2] * 1e3},
             "h2d_bytes_per_step": 8 * (ah.numel() + bh.numel()),
             "d2h_bytes_per_step": 8 * int(ch.numel()), "steps": steps,
-            "path": "tq_bs_create(host) x2 + tq_plan_create/execute + tq_bs_copy_data(host)"}
+            "host_result_equals_device_result": same,
+            "path": "tq_bs_set_data(host) x2 + tq_plan_create + tq_plan_execute_to(pinned host "
+                    "buffer: the GEMM writes the result over the host link as it runs)"}
 
 
 def main():

@@ -299,6 +299,17 @@ tq_status tq_plan_create(const tq_bs *A, const tq_bs *B, int32_t n_legs,
 /* Numeric stage: computes the result's data.  No host synchronisation, no
  * allocation: safe to capture in a CUDA graph.  A and B must be alive. */
 tq_status tq_plan_execute(tq_plan *plan, tq_stream stream);
+/* The numeric stage of tq_plan_execute with the result written to dst
+ * instead of the result tensor's own buffer (which is then not written).
+ * dst holds the result's n_elem elements in the result's layout and is
+ * device memory (TQ_MEM_DEVICE) or host memory (TQ_MEM_HOST).  Page-locked
+ * host memory (cudaHostAlloc, cudaHostRegister) is written by the kernels
+ * themselves over the host link while they run, so no device-to-host copy
+ * follows the GEMM; pageable host memory gets the computed result by one
+ * copy.  TQ_MEM_HOST synchronises the stream before returning.  The
+ * reference has no counterpart: its results are copied out of device memory
+ * (src/gpu/block_sparse.cuh:558-1026 leaves the result on the device). */
+tq_status tq_plan_execute_to(tq_plan *plan, void *dst, tq_memkind kind, tq_stream stream);
 /* Useful flops of the plan: sum over matched block pairs of 2*m*n*k. */
 tq_status tq_plan_flops(const tq_plan *plan, double *flops, int64_t *n_pairs);
 /* Record CUDA events on the launching stream around the phases of each

@@ -70,6 +70,7 @@ SIGNATURES = {
     "tq_nest_sum_noalloc": (ST, [P, I64, P, P, P]),
     "tq_plan_create": (ST, [P, P, I32, P64, P64, ctypes.POINTER(ContractOpts), P, PP, PP]),
     "tq_plan_execute": (ST, [P, P]),
+    "tq_plan_execute_to": (ST, [P, P, ctypes.c_int32, P]),
     "tq_plan_flops": (ST, [P, ctypes.POINTER(ctypes.c_double), P64]),
     "tq_plan_destroy": (ST, [P]),
     "tq_plan_set_profiling": (ST, [P, I32]),

@@ -194,6 +194,17 @@ class BlockSparseTensor:
                                          None))
         return out
 
+    def set_data(self, source_data, stream=None):
+        """Overwrite every element (tq_bs_set_data): a numpy array (host, copied
+        before return) or a torch CUDA tensor, n_elem elements of the tensor's
+        dtype in the tensor's layout."""
+        n = self.n_elem if self.rank else 1
+        data, kind = self._data_arg(source_data, self.dtype)
+        size = data.numel() if hasattr(data, "numel") else data.size
+        if size < n:
+            raise ValueError("source holds %d elements; the tensor has %d" % (size, n))
+        check(load().tq_bs_set_data(self._h, self._ptr(data), kind, _stream(stream)))
+
     def device_ptr(self) -> int:
         p = ctypes.c_void_p()
         check(load().tq_bs_device_data(self._h, ctypes.byref(p)))
@@ -442,6 +453,26 @@ class ContractionPlan:
     def execute(self, stream=None):
         check(load().tq_plan_execute(self._p, _stream(stream)))
         return self.result
+
+    def execute_to(self, dst, stream=None):
+        """Numeric stage with the result written into dst (tq_plan_execute_to):
+        a torch tensor on the GPU, a page-locked torch CPU tensor (written by
+        the kernels over the host link as they run) or a numpy array (one copy
+        after the GEMM).  dst holds result.n_elem elements of the result's
+        dtype; host destinations are complete on return."""
+        n = self.result.n_elem if self.result.rank else 1
+        dt = np.dtype(self.result.dtype)
+        if hasattr(dst, "data_ptr"):
+            ptr = dst.data_ptr()
+            kind = TQ_MEM_DEVICE if dst.is_cuda else TQ_MEM_HOST
+            size = dst.numel() * dst.element_size()
+        else:
+            if not (isinstance(dst, np.ndarray) and dst.flags.c_contiguous and dst.dtype == dt):
+                raise ValueError("dst must be a contiguous %s array" % dt)
+            ptr, kind, size = dst.ctypes.data, TQ_MEM_HOST, dst.nbytes
+        if size < n * dt.itemsize:
+            raise ValueError("dst holds %d bytes; the result needs %d" % (size, n * dt.itemsize))
+        check(load().tq_plan_execute_to(self._p, ctypes.c_void_p(ptr), kind, _stream(stream)))
 
     def check(self, stream=None):
         """Raise if a bounded device wait of the last execute gave up (syncs)."""

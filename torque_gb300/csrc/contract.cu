@@ -348,7 +348,7 @@ GemmJob make_gemm_job(const tq_plan *P) {
   job.perm = P->perm.p;
   job.tile_start = P->tile_start.p;
   job.c_off = P->C->d_meta.p ? P->C->d_meta.p + 3 * P->n_out * P->C->rank : nullptr;
-  job.C = P->C->data;
+  job.C = P->out ? P->out : P->C->data;
   job.n_out = P->n_out;
   job.chunks = nullptr;
   job.kfused = nullptr;
@@ -672,6 +672,7 @@ static tq_status plan_tc_classes(tq_plan *P, int32_t sl, int32_t tn, int64_t nex
   }
   OzJob &J = P->tc_job;
   J = OzJob{};
+  P->out = nullptr;  // a rebuilt job array writes the result tensor's buffer
   J.g = make_gemm_job(P);
   J.prs = P->pair_tab.p;
   J.tile_start = P->tc_tile_start.p;
@@ -814,6 +815,7 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
     S.rt_rows = k == 0 ? OZ_M : tn;
   }
   OzJob &J = P->tc_job;
+  P->out = nullptr;  // a rebuilt job array writes the result tensor's buffer
   J.g = make_gemm_job(P);
   J.tile_start = P->tc_tile_start.p;
   J.n_tiles = P->tc_tiles;
@@ -1076,9 +1078,30 @@ tq_status plan_reschedule(tq_plan *P, const tq_contract_opts &o, cudaStream_t s)
   return TQ_OK;
 }
 
-tq_status plan_run(tq_plan *P, cudaStream_t s) {
+// The tensor-core job array lives on the device: its output pointer is
+// rewritten there (one thread), in stream order.
+__global__ void set_job_output_kernel(OzJob *jobs, void *c) { jobs[0].g.C = c; }
+
+// Points the numeric stage's writes at out (device-addressable), or back at
+// the result tensor's buffer when out is null.
+static tq_status plan_bind_output(tq_plan *P, void *out, cudaStream_t s) {
+  if (P->out == out) return TQ_OK;
+  P->out = out;
+  if (P->tc && P->tcb.jobs.p) {
+    count_launch(), set_job_output_kernel<<<1, 1, 0, s>>>(P->tcb.jobs.p, out ? out : P->C->data);
+    TQ_CUDA(cudaGetLastError());
+  }
+  return TQ_OK;
+}
+
+static tq_status plan_run_to(tq_plan *P, void *out, cudaStream_t s);
+
+tq_status plan_run(tq_plan *P, cudaStream_t s) { return plan_run_to(P, nullptr, s); }
+
+static tq_status plan_run_to(tq_plan *P, void *out, cudaStream_t s) {
   if (!P->sched_ok)
     return fail(TQ_ERR_INVALID, "the plan's last reschedule failed; give it a valid schedule");
+  TQ_CHECK(plan_bind_output(P, out, s));
   const GemmJob job = make_gemm_job(P);
   if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[0], s));
   tq_status st = TQ_OK;
@@ -1117,6 +1140,32 @@ tq_status tq_plan_create(const tq_bs *A, const tq_bs *B, int32_t n_legs, const i
 tq_status tq_plan_execute(tq_plan *plan, tq_stream stream) {
   if (!plan) return fail(TQ_ERR_INVALID, "plan is NULL");
   return plan_run(plan, (cudaStream_t)stream);
+}
+
+tq_status tq_plan_execute_to(tq_plan *plan, void *dst, tq_memkind kind, tq_stream stream) {
+  if (!plan || !dst) return fail(TQ_ERR_INVALID, "NULL argument");
+  if (kind != TQ_MEM_HOST && kind != TQ_MEM_DEVICE) return fail(TQ_ERR_INVALID, "bad memory kind");
+  cudaStream_t s = (cudaStream_t)stream;
+  tq_plan *P = plan;
+  void *dev = kind == TQ_MEM_DEVICE ? dst : nullptr;
+  if (kind == TQ_MEM_HOST && P->C->rank > 0) {
+    // page-locked host memory is addressable by the kernels (unified
+    // addressing): they write it over the host link as they go
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, dst) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+        a.devicePointer)
+      dev = a.devicePointer;
+    else
+      (void)cudaGetLastError();
+  }
+  if (dev) {
+    TQ_CHECK(plan_run_to(P, dev, s));
+    if (kind == TQ_MEM_HOST) TQ_CUDA(cudaStreamSynchronize(s));
+    return TQ_OK;
+  }
+  // pageable host memory (or a rank-0 result): compute, then one copy
+  TQ_CHECK(plan_run(P, s));
+  return tq_bs_copy_data(P->C, dst, kind, stream);
 }
 
 tq_status tq_plan_reschedule(tq_plan *plan, const tq_contract_opts *opts, tq_stream stream) {

@@ -20,6 +20,7 @@ struct NativeWorkDev {
 struct tq_plan {
   const tq_bs *A = nullptr, *B = nullptr;
   tq_bs *C = nullptr;  // owned by the caller
+  void *out = nullptr; // where the numeric stage writes (null: C's own buffer)
   tq::LegSpec L;
   tq_contract_opts opts;
   int64_t n_pairs = 0, n_out = 0, n_tiles = 0, n_chunks = 0;
