@@ -14,7 +14,7 @@ TQ_OK, TQ_ERR_INVALID, TQ_ERR_CUDA, TQ_ERR_OOM, TQ_ERR_RANGE, TQ_ERR_UNSUPPORTED
     TQ_ERR_TIMEOUT = range(7)
 TQ_F32, TQ_F64, TQ_F16 = 0, 1, 2
 TQ_MEM_HOST, TQ_MEM_DEVICE = 0, 1
-PRECISIONS = {"native": 0, "fp64": 0, "ozaki": 1, "bf16x3": 2}
+PRECISIONS = {"native": 0, "fp64": 0, "ozaki": 1, "bf16x3": 2, "tensor": 3}
 LAYOUTS = {"reference": 0, "reduced": 1}
 
 # Every exported symbol of include/torque_gb300.h with its ctypes signature.

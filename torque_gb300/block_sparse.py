@@ -424,7 +424,7 @@ def contract_blocks(A: "BlockSparseTensor", B: "BlockSparseTensor", contracting_
 
 
 def make_opts(precision="native", layout="reference", slices=0, tile_n=0, native_fill=0):
-    """tq_contract_opts from names: precision native|ozaki|bf16x3, layout
+    """tq_contract_opts from names: precision native|ozaki|bf16x3|tensor, layout
     reference|reduced; slices, tile_n (32/64/96) and native_fill (per mille)
     apply to the tensor-core forms."""
     return ContractOpts(_lib.PRECISIONS[precision], _lib.LAYOUTS[layout], int(slices), int(tile_n),

@@ -373,6 +373,7 @@ static OzSide make_side(const tq_bs *T, int32_t nfree, const int32_t *fl, int32_
   S.row_start = row_start;
   S.tile_start = tile_start;
   S.unit_off = unit_off;
+  S.f16 = T->dtype == TQ_F16;
   return S;
 }
 
@@ -674,6 +675,7 @@ static tq_status plan_tc_classes(tq_plan *P, int32_t sl, int32_t tn, int64_t nex
   J = OzJob{};
   P->out = nullptr;  // a rebuilt job array writes the result tensor's buffer
   J.g = make_gemm_job(P);
+  J.f16 = P->A->dtype == TQ_F16;
   J.prs = P->pair_tab.p;
   J.tile_start = P->tc_tile_start.p;
   J.n_tiles = P->tc_tiles;
@@ -701,6 +703,11 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   const LegSpec &L = P->L;
   const tq_bs *A = P->A, *B = P->B;
   int32_t sl = P->opts.slices;
+  if (P->opts.precision == TQ_PREC_TENSOR) {
+    // binary16 operands go to the tensor cores as they are: one "slice"
+    if (sl > 1) return fail(TQ_ERR_INVALID, "the tensor form has no slices");
+    sl = 1;
+  }
   if (sl == 0) sl = P->opts.precision == TQ_PREC_OZAKI ? 5 : 3;
   if (sl < 1 || sl > OZ_MAXS) return fail(TQ_ERR_INVALID, "slice count outside 1..7");
   P->slices = sl;
@@ -817,6 +824,7 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   OzJob &J = P->tc_job;
   P->out = nullptr;  // a rebuilt job array writes the result tensor's buffer
   J.g = make_gemm_job(P);
+  J.f16 = P->A->dtype == TQ_F16;
   J.tile_start = P->tc_tile_start.p;
   J.n_tiles = P->tc_tiles;
   J.ksum = P->ksum.p;
@@ -853,6 +861,18 @@ static tq_status run_tc(tq_plan *P, cudaStream_t s) {
   if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[1], s));
   if (P->tc_tiles) TQ_CHECK(oz_batch_gemm(P->tcb, s));
   return run_hybrid_native(P, s);
+}
+
+// The sliced forms take float64 tensors; the tensor form takes binary16 ones.
+static tq_status check_precision(int32_t precision, tq_dtype dtype) {
+  if (precision != TQ_PREC_NATIVE && precision != TQ_PREC_OZAKI && precision != TQ_PREC_BF16X3 &&
+      precision != TQ_PREC_TENSOR)
+    return fail(TQ_ERR_INVALID, "unknown precision");
+  if ((precision == TQ_PREC_OZAKI || precision == TQ_PREC_BF16X3) && dtype != TQ_F64)
+    return fail(TQ_ERR_UNSUPPORTED, "the sliced tensor-core forms take float64 tensors");
+  if (precision == TQ_PREC_TENSOR && dtype != TQ_F16)
+    return fail(TQ_ERR_UNSUPPORTED, "the tensor form takes half tensors");
+  return TQ_OK;
 }
 
 tq_status validate_legs(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,
@@ -894,11 +914,7 @@ tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64
   TQ_CHECK(validate_legs(A, B, n_legs, a_legs, b_legs, L));
   tq_contract_opts o = {TQ_PREC_NATIVE, TQ_LAYOUT_REFERENCE, 0, 0, 0, 0};
   if (opts) o = *opts;
-  if (o.precision != TQ_PREC_NATIVE && o.precision != TQ_PREC_OZAKI &&
-      o.precision != TQ_PREC_BF16X3)
-    return fail(TQ_ERR_INVALID, "unknown precision");
-  if (o.precision != TQ_PREC_NATIVE && A->dtype != TQ_F64)
-    return fail(TQ_ERR_UNSUPPORTED, "tensor-core forms take float64 tensors");
+  TQ_CHECK(check_precision(o.precision, A->dtype));
   if (o.layout != TQ_LAYOUT_REFERENCE && o.layout != TQ_LAYOUT_REDUCED)
     return fail(TQ_ERR_INVALID, "unknown layout");
   TQ_CHECK(sync_device_meta(const_cast<tq_bs *>(A), s));
@@ -1055,12 +1071,8 @@ tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64
 // A new schedule (precision, slices, tile width, grouping) for a planned
 // contraction: the symbolic stage is kept, only the tensor-core part is rebuilt.
 tq_status plan_reschedule(tq_plan *P, const tq_contract_opts &o, cudaStream_t s) {
-  if (o.precision != TQ_PREC_NATIVE && o.precision != TQ_PREC_OZAKI &&
-      o.precision != TQ_PREC_BF16X3)
-    return fail(TQ_ERR_INVALID, "unknown precision");
+  TQ_CHECK(check_precision(o.precision, P->A->dtype));
   if (o.layout != P->opts.layout) return fail(TQ_ERR_INVALID, "a new schedule keeps the layout");
-  if (o.precision != TQ_PREC_NATIVE && P->A->dtype != TQ_F64)
-    return fail(TQ_ERR_UNSUPPORTED, "tensor-core forms take float64 tensors");
   const bool tc = o.precision != TQ_PREC_NATIVE && P->C->rank > 0 && P->n_pairs > 0;
   if (tc && !P->keys)
     return fail(TQ_ERR_INVALID,

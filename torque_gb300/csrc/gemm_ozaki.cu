@@ -36,6 +36,7 @@
 // (K-major, no swizzle, LBO = 128 B along K, SBO = 256 B along M/N), so one
 // bulk copy per operand per k-step fills a pipeline stage.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <atomic>
 
@@ -86,6 +87,7 @@ __global__ void oz_rowexp_kernel(OzLaunch L) {
   if (g >= L.n_rows) return;
   const int64_t k = oz_find(L.side_row_start, L.n_sides, g);
   const OzSide &S = L.sides[k];
+  if (S.f16) return;  // binary16 operands are not scaled
   const int64_t lr = g - L.side_row_start[k];
   const int64_t b = oz_find(S.row_start, S.T.nb, lr);
   const int64_t r = lr - S.row_start[b];
@@ -174,6 +176,23 @@ __device__ __forceinline__ void oz_slice_kstep(const double *d, bool row_ok, int
   }
 }
 
+// Binary16 operands as they are: the 8 half values of half row c of row r in
+// k-step q, in the same core-matrix image (one slice).
+__device__ __forceinline__ void oz_copy_kstep_f16(const __half *d, bool row_ok, int64_t ra,
+                                                  const Operand &op, int64_t q, int c, int G,
+                                                  int r, uint8_t *chunk) {
+  uint32_t packed[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int x = 0; x < 8; x++) {
+    const int64_t kk = q * 16 + c * 8 + x;
+    uint32_t h = 0;
+    if (row_ok && kk < op.cols) h = __half_as_ushort(d[ra + mixed_addr(kk, op.nc, op.cdim, op.cst)]);
+    packed[x >> 1] |= h << (16 * (x & 1));
+  }
+  *(uint4 *)(chunk + ((r / 8) * 2 + c) * 128 + (r % 8) * 16) =
+      make_uint4(packed[0], packed[1], packed[2], packed[3]);
+}
+
 // Class layout: one work item is a row tile of a class times one of its
 // contracted boxes; the tile's rows come from the blocks of several free boxes.
 __device__ __forceinline__ void oz_slice_class(const OzSide &S, int64_t lt) {
@@ -197,6 +216,12 @@ __device__ __forceinline__ void oz_slice_class(const OzSide &S, int64_t lt) {
     e = S.exps[vr];
   }
   uint8_t *base = S.slices + 256 * it.unit + (int64_t)it.koff * s * G * 256;
+  if (S.f16) {
+    for (int64_t q = 0; q < it.nk; q++)
+      oz_copy_kstep_f16((const __half *)S.T.data, row_ok, ra, op, q, c, G, r,
+                        base + q * (int64_t)G * 256);
+    return;
+  }
   const double *d = (const double *)S.T.data;
   for (int64_t q = 0; q < it.nk; q++)
     oz_slice_kstep(d, row_ok, ra, op, q, c, 8 * s - e, s, G, r, base + q * (int64_t)s * G * 256);
@@ -227,8 +252,14 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OzLaunch L) {
   if (r >= G * 8) return;
   const int64_t grow = rt * rt_rows + r;
   const bool row_ok = r < rows;
-  const int e = row_ok ? S.exps[S.row_off[S.key[b]] + grow] : OZ_EXP_ZERO;
   const int64_t ra = row_ok ? op.base + mixed_addr(grow, op.nr, op.rdim, op.rst) : 0;
+  if (S.f16) {
+    for (int64_t q = 0; q < nk; q++)
+      oz_copy_kstep_f16((const __half *)S.T.data, row_ok, ra, op, q, c, G, r,
+                        base + q * (int64_t)G * 256);
+    return;
+  }
+  const int e = row_ok ? S.exps[S.row_off[S.key[b]] + grow] : OZ_EXP_ZERO;
   for (int64_t q = 0; q < nk; q++)
     oz_slice_kstep(d, row_ok, ra, op, q, c, 8 * s - e, s, G, r, base + q * (int64_t)s * G * 256);
 }
@@ -351,7 +382,10 @@ tq_status oz_batch_build(const std::vector<OzJob> &jobs, const std::vector<OzSid
   int64_t *jt = pre.data(), *sr = jt + nj + 1, *stl = sr + ns + 1, *se = stl + ns + 1;
   int s_max = 1;
   const int tile_n = nj ? jobs[0].tile_n : OZ_N;
+  const int32_t f16 = nj ? jobs[0].f16 : 0;
   for (int64_t j = 0; j < nj; j++) {
+    if (jobs[j].f16 != f16)
+      return fail(TQ_ERR_UNSUPPORTED, "binary16 and float64 jobs cannot share a tensor-core launch");
     jt[j + 1] = jt[j] + jobs[j].n_tiles;
     s_max = jobs[j].s > s_max ? jobs[j].s : s_max;
     if (jobs[j].tile_n != tile_n)
@@ -393,6 +427,7 @@ tq_status oz_batch_build(const std::vector<OzJob> &jobs, const std::vector<OzSid
   for (int64_t j = 0; j < nj; j++)
     if (jobs[j].s != s_max) L.s_all = 0;
   L.tile_n = tile_n;
+  L.f16 = f16;
   L.nstages = oz_stages(s_max, tile_n);
   L.err = out.err.p;
   debug_waits(&L.wait_ns, &L.delay_ns);
@@ -435,6 +470,7 @@ static tq_status oz_setup(int *sms) {
     TQ_CHECK(oz_gemm_set_attr_s0());
     TQ_CHECK(oz_gemm_set_attr_s3());
     TQ_CHECK(oz_gemm_set_attr_s5());
+    TQ_CHECK(oz_gemm_set_attr_f16());
     g_sms[dev] = n;
   }
   *sms = g_sms[dev];
@@ -446,6 +482,7 @@ tq_status oz_batch_gemm(const OzBatchDev &b, cudaStream_t st) {
   if (L.n_tiles == 0) return TQ_OK;
   const int64_t grid = L.n_tiles < b.sms ? L.n_tiles : b.sms;
   count_launch();
+  if (L.f16) return oz_gemm_run_f16(L, (unsigned)grid, st);
   // straight-line issue code when every job of the launch has 3 or 5 slices
   if (L.s_all == 5) return oz_gemm_run_s5(L, (unsigned)grid, st);
   if (L.s_all == 3) return oz_gemm_run_s3(L, (unsigned)grid, st);

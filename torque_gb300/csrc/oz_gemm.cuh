@@ -4,6 +4,9 @@
 // translation units, which compile in parallel.
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <type_traits>
 
 #include "gemm.cuh"
 #include "ozaki.cuh"
@@ -214,7 +217,12 @@ __device__ __forceinline__ void oz_unpack(const OzLaunch &L, const OzTileRec &r,
 }
 
 // S > 0: every job of the launch has S slices (straight-line issue code);
-// S = 0: any slice count (dispatched per job).
+// S = 0: any slice count (dispatched per job); S = OZ_F16: binary16 operands
+// taken as they are (one "slice", kind::f16 with fp16 A and B, fp32
+// accumulation in TMEM, retired accumulators summed in FP64, one rounding of
+// each result element to binary16).
+constexpr int OZ_F16 = -1;
+
 template <int N, int S>
 __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -374,7 +382,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         const int s = J.s;
         const int n_acc = s < OZ_NACC ? s : OZ_NACC;
         const OzPairRec *prs = J.prs;
-        const uint32_t idesc = idesc_bf16_f32(OZ_M, (uint32_t)T.nmma);
+        const uint32_t idesc = S == OZ_F16 ? idesc_f16_f32(OZ_M, (uint32_t)T.nmma)
+                                           : idesc_bf16_f32(OZ_M, (uint32_t)T.nmma);
         OzSchedule sch;
         sch.start(T.ksum, n_acc);
         int64_t ev_k;
@@ -404,6 +413,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
             if (elect_one()) {
               if constexpr (S > 0)
                 oz_issue<S, true, OzSlots<N>::ntm>(col, dA0 + so, dB0 + so, (uint32_t)T.ga * 16,
+                                                   (uint32_t)T.gb * 16, idesc, fresh,
+                                                   tmem + NSLOT * N);
+              else if constexpr (S == OZ_F16)
+                oz_issue<1, true, OzSlots<N>::ntm>(col, dA0 + so, dB0 + so, (uint32_t)T.ga * 16,
                                                    (uint32_t)T.gb * 16, idesc, fresh,
                                                    tmem + NSLOT * N);
               else
@@ -459,16 +472,17 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       const int n_acc = J.s < OZ_NACC ? J.s : OZ_NACC;
       const int64_t grow = T.mt * OZ_M + row;
       const bool row_ok = grow < T.m;
-      const int er = row_ok ? J.expA[T.erow + grow] : 0;
+      const int er = S != OZ_F16 && row_ok ? J.expA[T.erow + grow] : 0;
       // S: running sum in units of 2^-u of the leading slice product.  With
       // u <= 48 - log2(K) the sum stays below 2^62.1 for any data, and u >= 24
       // keeps D0..D2 (whole multiples of 2^-16) exact.
       int kb = 0;
       while (kb < 40 && (int64_t(1) << kb) < 16 * T.ksum) kb++;
       const int u = 48 - kb < 32 ? 48 - kb : 32;
-      long long S[N / 2];
+      // binary16 operands: a plain sum of the fp32 accumulators, in FP64
+      std::conditional_t<S == OZ_F16, double, long long> sum[N / 2];
 #pragma unroll
-      for (int y = 0; y < N / 2; y++) S[y] = 0;
+      for (int y = 0; y < N / 2; y++) sum[y] = 0;
       OzSchedule sch;
       sch.start(T.ksum, n_acc);
       bool done = false;
@@ -504,14 +518,43 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
 #pragma unroll
           for (int x = 0; x < N / 16; x++)
 #pragma unroll
-            for (int y = 0; y < 8; y++)
-              S[8 * x + y] += (long long)oz_to_int(__uint_as_float(v[x][y]), scale) << shift;
+            for (int y = 0; y < 8; y++) {
+              if constexpr (S == OZ_F16)
+                sum[8 * x + y] += (double)__uint_as_float(v[x][y]);
+              else
+                sum[8 * x + y] += (long long)oz_to_int(__uint_as_float(v[x][y]), scale) << shift;
+            }
           sm.retire(a);
           if (!done) sch.advance(a);
         }
       }
       if (abort_flag) break;
-      // C = S * 2^(e_r + f_c - 16 - u)
+      if constexpr (S == OZ_F16) {
+        // binary16 result: each element rounded once from the FP64 sum
+        __half *C = (__half *)J.g.C + T.c_off;
+        if (J.cls) {
+          if (row_ok) {
+            const OzRowMap ra_ = J.rmapA[T.erow + grow];
+#pragma unroll
+            for (int y = 0; y < N / 2; y++) {
+              const int64_t gcol = T.nt * N + cbase + y;
+              if (gcol < T.n) {
+                const OzRowMap cb = J.rmapB[T.ecol + gcol];
+                C[__ldg(J.offs + ra_.xoff + cb.xi) + ra_.xr + (int64_t)cb.xr * ra_.m] =
+                    __double2half(sum[y]);
+              }
+            }
+          }
+        } else if (row_ok) {
+#pragma unroll
+          for (int y = 0; y < N / 2; y++) {
+            const int64_t gcol = T.nt * N + cbase + y;
+            if (gcol < T.n) C[grow + gcol * T.m] = __double2half(sum[y]);
+          }
+        }
+        continue;
+      }
+      // C = sum * 2^(e_r + f_c - 16 - u)
       double *C = (double *)J.g.C + T.c_off;
       const int64_t rowB = T.ecol;
       const int32_t *expB = J.expB;
@@ -538,7 +581,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
             }
 #pragma unroll
             for (int y = 0; y < 8; y++)
-              if (dst[y] >= 0) C[dst[y]] = oz_i64_ldexp(S[y0 + y], er + fc[y] - 16 - u);
+              if (dst[y] >= 0) C[dst[y]] = oz_i64_ldexp(sum[y0 + y], er + fc[y] - 16 - u);
           }
         }
       } else if (row_ok) {
@@ -555,7 +598,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
 #pragma unroll
           for (int y = 0; y < 8; y++) {
             const int64_t gcol = T.nt * N + cbase + y0 + y;
-            if (gcol < T.n) C[grow + gcol * T.m] = oz_i64_ldexp(S[y0 + y], er + fc[y] - 16 - u);
+            if (gcol < T.n) C[grow + gcol * T.m] = oz_i64_ldexp(sum[y0 + y], er + fc[y] - 16 - u);
           }
         }
       }
@@ -592,13 +635,15 @@ tq_status oz_gemm_run(const OzLaunch &L, unsigned grid, cudaStream_t st) {
   return TQ_OK;
 }
 
-// The instantiations: S = 0 (any slice count), 3 (three-way bf16) and 5 (the
-// FP64-level default), one translation unit each.
+// The instantiations: S = 0 (any slice count), 3 (three-way bf16), 5 (the
+// FP64-level default) and OZ_F16 (binary16 operands), one translation unit each.
 tq_status oz_gemm_set_attr_s0();
 tq_status oz_gemm_set_attr_s3();
 tq_status oz_gemm_set_attr_s5();
 tq_status oz_gemm_run_s0(const OzLaunch &L, unsigned grid, cudaStream_t st);
 tq_status oz_gemm_run_s3(const OzLaunch &L, unsigned grid, cudaStream_t st);
 tq_status oz_gemm_run_s5(const OzLaunch &L, unsigned grid, cudaStream_t st);
+tq_status oz_gemm_set_attr_f16();
+tq_status oz_gemm_run_f16(const OzLaunch &L, unsigned grid, cudaStream_t st);
 
 }  // namespace tq

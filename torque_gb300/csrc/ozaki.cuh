@@ -64,6 +64,7 @@ struct OzSide {
   uint8_t *slices;            // slice storage
   int64_t n_rows, n_tiles, n_exps;
   int32_t s, rt_rows;
+  int32_t f16;                // binary16 data: copied as they are (one slice, no exponents)
   // class layout (items != NULL): n_tiles counts the items
   const OzClassItem *items;
   const OzRowMap *rmap;       // per virtual row
@@ -92,6 +93,7 @@ struct OzJob {
   const int32_t *expA, *expB;
   int32_t s;
   int32_t tile_n;             // output columns per tile (every job of a launch alike)
+  int32_t f16;                // binary16 operands and result, fp32 accumulation (s = 1)
   // class layout (cls != NULL): the GEMM's outputs are the classes, each with one
   // pseudo-pair (its whole contracted range); tile_start and ksum are per class
   const OzClassOut *cls;
@@ -126,6 +128,7 @@ struct OzLaunch {
   int64_t n_rows, n_slice_tiles, n_exps;
   int32_t s_max, nstages, tile_n;
   int32_t s_all;           // the slice count of every job, or 0 when they differ
+  int32_t f16;             // every job has binary16 operands (jobs of one launch agree)
   int32_t *err;
   const OzTileRec *tiles;  // [n_tiles]
   uint64_t wait_ns;        // limit of every pipeline wait (nanoseconds of wall time)
