@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--no-hbm", action="store_true")
     p.add_argument("--no-costmodel", action="store_true")
     p.add_argument("--no-sparse", action="store_true")
+    p.add_argument("--no-half", action="store_true")
     return p.parse_args()
 
 
@@ -270,8 +271,10 @@ def sampled_error(c, a_dev, b_dev, C, n_largest=2, n_random=4, seed=5):
             i, j = int(pa[q]), int(pb[q])
             kk = int(np.prod(da[i, 2:]))
             kf += kk
-            am = a_dev[int(oa[i]):int(oa[i] + sa[i])].cpu().numpy().reshape((m, kk), order="F")
-            bm = b_dev[int(ob[j]):int(ob[j] + sb[j])].cpu().numpy().reshape((kk, n), order="F")
+            am = a_dev[int(oa[i]):int(oa[i] + sa[i])].double().cpu().numpy().reshape((m, kk),
+                                                                                     order="F")
+            bm = b_dev[int(ob[j]):int(ob[j] + sb[j])].double().cpu().numpy().reshape((kk, n),
+                                                                                     order="F")
             want += am @ bm
             mag += np.abs(am) @ np.abs(bm)
         largest_k = max(largest_k, kf)
@@ -289,19 +292,20 @@ def sampled_error(c, a_dev, b_dev, C, n_largest=2, n_random=4, seed=5):
 
 
 def block_data(C, offset, n):
-    """Host copy of n elements of C's device data starting at `offset`."""
+    """Host copy (float64) of n elements of C's device data starting at `offset`."""
     import torch
     torch.cuda.synchronize()
-    return _ptr_tensor(C.device_ptr() + 8 * offset, n).cpu().numpy()
+    dt = np.dtype(C.dtype)
+    return _ptr_tensor(C.device_ptr() + dt.itemsize * offset, n, dt).cpu().double().numpy()
 
 
-def _ptr_tensor(ptr, n):
-    """A float64 CUDA tensor viewing n elements at device address ptr (no copy)."""
+def _ptr_tensor(ptr, n, dtype=np.float64):
+    """A CUDA tensor viewing n elements of `dtype` at device address ptr (no copy)."""
     import torch
 
     class _Holder:
-        __cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False),
-                                    "version": 2}
+        __cuda_array_interface__ = {"shape": (n,), "typestr": np.dtype(dtype).str,
+                                    "data": (ptr, False), "version": 2}
     return torch.as_tensor(_Holder(), device="cuda")
 
 
@@ -503,6 +507,8 @@ def run_ours(args):
             del P
         if not args.no_hbm:
             line["hbm_kernels"] = hbm_kernels(tq, c, A, B)
+        if not args.no_half:
+            line["half_tensor"] = half_tensor(tq, c, a, b)
         line["cpu_baseline"] = dict(zip(("value", "cores", "sample"),
                                         cpu_sample(c, a, b, args.cpu_seconds)))
         line["cpu_baseline"].update({"unit": "TFLOP/s", "kind": "port"})
@@ -521,6 +527,45 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def half_tensor(tq, c, a, b, reps=3):
+    """The headline contraction in half precision: the float64 inputs rounded
+    to binary16, reduced layout; precision "tensor" (fp16 products on the
+    tcgen05 tensor cores, fp32 accumulation, one rounding of each result) timed
+    against the plain half path (FP32 SIMT accumulation) on the same tensors.
+    Times: CUDA events around the numeric stage on the launching stream;
+    accuracy: sampled output blocks against float64 products of the rounded
+    inputs."""
+    import torch
+    a16, b16 = a.half(), b.half()
+    A = tq.BlockSparseTensor(c.A.dimension, a16, c.A.begin.T, c.A.end.T, dtype=np.float16)
+    B = tq.BlockSparseTensor(c.B.dimension, b16, c.B.begin.T, c.B.end.T, dtype=np.float16)
+    out = {"dtype": "f16 operands and result, f32 accumulation"}
+    for name, prec, n in (("tensor", "tensor", reps), ("native", "native", 1)):
+        P = tq.ContractionPlan(A, B, c.pairs, precision=prec, layout="reduced")
+        P.set_profiling(True)
+        P.execute()
+        P.check()
+        ts, gm = [], []
+        for _ in range(n):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            P.execute()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+            gm.append(P.last_timings()[1])
+        ms = statistics.median(ts)
+        out[name] = {"ms": ms, "tflops": P.flops / (ms / 1e3) / 1e12,
+                     "gemm_ms": statistics.median(gm)}
+        if name == "tensor":
+            out[name]["error"] = sampled_error(c, a16, b16, P.result)
+        del P
+    out["speedup_tensor_vs_native"] = out["native"]["ms"] / out["tensor"]["ms"]
+    del A, B
+    return out
 
 
 def hbm_kernels(tq, c, A, B):
@@ -849,14 +894,6 @@ def cost_model(tq, n_live=200):
     return out
 
 
-class _DeviceView:
-    """A raw device pointer seen by torch (no copy): __cuda_array_interface__."""
-
-    def __init__(self, ptr, n):
-        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False),
-                                         "version": 3}
-
-
 def e2e(tq, c, ah, bh, kw, steps, ch=None):
     """The same contraction through the C ABI from pinned host buffers, every
     step: both inputs copied from host memory into the operand tensors
@@ -891,8 +928,7 @@ def e2e(tq, c, ah, bh, kw, steps, ch=None):
         fl = P.flops
         if s == steps:
             P.execute()
-            dev = torch.as_tensor(_DeviceView(P.result.device_ptr(), P.result.n_elem),
-                                  device="cuda")
+            dev = _ptr_tensor(P.result.device_ptr(), P.result.n_elem)
             same = bool(torch.equal(dev, ch[:P.result.n_elem].to("cuda", non_blocking=False)))
         del P
         if s > 0:  # the first pass pins pages and warms the allocator
