@@ -480,8 +480,12 @@ def run_ours(args):
         line["roofline"] = roof
 
         if not args.no_e2e:
-            # right after the device-resident steps, in the same GPU state (the
-            # device-resident inputs stay allocated for the legs below)
+            # right after the device-resident steps (the device-resident inputs
+            # stay allocated for the legs below).  The pool's cached memory is
+            # returned first: after the tile-width tuning has cycled tens of GB
+            # through it, copies into buffers carved from that memory ran at a
+            # quarter of the link's rate
+            _lib.check(lib.tq_release_cached_memory())
             ah, bh, ch = pinned
             ah.copy_(a)
             bh.copy_(b)

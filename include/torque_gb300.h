@@ -264,6 +264,15 @@ tq_status tq_bs_create_charges(tq_dtype dtype, int32_t rank, const int64_t *n_se
 tq_status tq_bs_svd(const tq_bs *t, int32_t n_row_legs, const int64_t *row_legs,
                     int64_t max_keep, double cutoff, tq_stream stream, tq_bs **U, tq_bs **S,
                     tq_bs **V);
+/* Block-level QR (an extension, same class structure as tq_bs_svd): each
+ * class matrix A (M x N) is factored by Householder reflections in FP64 on the
+ * device as A = Q R with Q (M x k, orthonormal columns), R (k x N, upper
+ * trapezoidal, non-negative diagonal), k = min(M, N).  Returns Q[row legs...,
+ * bond] and R[bond, column legs...] over a new bond leg with one sector of k
+ * per class (classes in the order of their first row box), so that T =
+ * sum_k Q[..., k] R[k, ...].  float64 tensors of sector boxes. */
+tq_status tq_bs_qr(const tq_bs *t, int32_t n_row_legs, const int64_t *row_legs, tq_stream stream,
+                   tq_bs **Q, tq_bs **R);
 
 /* slice (block_sparse.cuh:1124-1176): split every block into prod(divisor)
  * boxes without moving data, as the reference does. */

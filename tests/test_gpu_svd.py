@@ -67,3 +67,47 @@ def test_svd_truncation(tq, keep):
     U2, S2, V2 = T.svd([0, 1], cutoff=0.3)
     assert np.array_equal(np.sort(S2.data())[::-1], np.sort(S2.data())[::-1])
     assert S2.data().size == int(np.sum(full > 0.3 * full[0]))
+
+
+@pytest.mark.parametrize("row_legs", [[0, 1], [2, 0], [3], [0, 1, 3]])
+def test_qr(tq, row_legs):
+    """Q R reproduces the tensor, Q has orthonormal columns, and each class's
+    R (its blocks side by side, in the order the library emits them) is upper
+    trapezoidal with a non-negative diagonal; R = Q^T A."""
+    T = site(tq, 6)
+    D = dense(T)
+    Q, R = T.qr(row_legs)
+    cols = [l for l in range(4) if l not in row_legs]
+    rs = int(np.prod([D.shape[l] for l in row_legs]))
+    mat = np.transpose(D, row_legs + cols).reshape(rs, -1, order="F")
+    q, rr = dense(Q), dense(R)
+    k = q.shape[-1]
+    qm = q.reshape(rs, k, order="F")
+    rm = rr.reshape(k, -1, order="F")
+    assert np.max(np.abs(qm.T @ qm - np.eye(k))) <= 1e-12
+    assert np.max(np.abs(qm @ rm - mat)) <= 1e-12 * np.max(np.abs(mat))
+    assert np.max(np.abs(qm.T @ mat - rm)) <= 1e-12 * np.max(np.abs(mat))
+    # per class: R's blocks of one bond sector, side by side
+    dim, b, e, t, o = R.metadata()
+    data = R.data()
+    sectors = {}
+    for blk in range(b.shape[1]):
+        sectors.setdefault(int(b[0, blk]), []).append(blk)
+    assert sum(int(e[0, v[0]] - b[0, v[0]] + 1) for v in sectors.values()) == k
+    for lo, blks in sectors.items():
+        kc = int(e[0, blks[0]] - lo + 1)
+        parts = []
+        for blk in blks:
+            n = int(np.prod(e[1:, blk] - b[1:, blk] + 1))
+            parts.append(data[o[blk]:o[blk] + kc * n].reshape(kc, n, order="F"))
+        rc = np.concatenate(parts, axis=1)
+        assert np.all(np.tril(rc, -1) == 0.0)
+        assert np.all(np.diag(rc) >= 0.0)
+
+
+def test_qr_rejects_bad_legs(tq):
+    T = site(tq, 7)
+    with pytest.raises(tq.TorqueError):
+        T.qr([])
+    with pytest.raises(tq.TorqueError):
+        T.qr([0, 1, 2, 3])

@@ -57,6 +57,7 @@ SIGNATURES = {
     "tq_bs_split_leg": (ST, [P, I32, I64, P64, I64, P64, P64, P, PP]),
     "tq_bs_contract_elements": (ST, [P, P, I32, P64, P64, P, PP]),
     "tq_bs_svd": (ST, [P, I32, P64, I64, ctypes.c_double, P, PP, PP, PP]),
+    "tq_bs_qr": (ST, [P, I32, P64, P, PP, PP]),
     "tq_charge_blocks": (ST, [I32, P64, P64, P64, ctypes.POINTER(ctypes.c_int32), I64, I64, I64,
                               P64, P64, P64]),
     "tq_bs_create_charges": (ST, [I32, I32, P64, P64, P64, ctypes.POINTER(ctypes.c_int32), I64,

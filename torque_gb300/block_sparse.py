@@ -339,6 +339,16 @@ class BlockSparseTensor:
         return (BlockSparseTensor(_handle=u), BlockSparseTensor(_handle=sv),
                 BlockSparseTensor(_handle=v))
 
+    def qr(self, row_legs, stream=None):
+        """Block-level QR (tq_bs_qr): row_legs against the other legs; returns
+        (Q[row legs..., bond], R[bond, other legs...]), each class factored as
+        Q R with orthonormal Q columns and R upper trapezoidal, diagonal >= 0."""
+        rl = _i64(row_legs)
+        q, r = ctypes.c_void_p(), ctypes.c_void_p()
+        check(load().tq_bs_qr(self._h, rl.size, _p64(rl), _stream(stream), ctypes.byref(q),
+                              ctypes.byref(r)))
+        return BlockSparseTensor(_handle=q), BlockSparseTensor(_handle=r)
+
     def slice(self, divisor, stream=None) -> "BlockSparseTensor":
         d = _i64(divisor)
         h = ctypes.c_void_p()

@@ -1,5 +1,5 @@
-// Block-level truncated SVD of a block-sparse tensor (the step after the
-// contraction in PEPS / MPS sweeps; the reference has only a cuSOLVER QR
+// Block-level truncated SVD and QR of a block-sparse tensor (the step after
+// the contraction in PEPS / MPS sweeps; the reference has only a cuSOLVER QR
 // example that nothing calls, test/cusolver_playground.cpp:7).
 //
 // The legs are split into row legs (given) and column legs (the rest, in
@@ -200,6 +200,219 @@ __global__ void svd_scatter_kernel(const SvdOut *ob, const int64_t *ostart, int6
   }
 }
 
+
+// ---------------------------------------------------------------- QR
+// Householder QR of one class per CTA (FP64): A (m x n, ld m) becomes R in
+// its upper triangle and the reflector vectors below it (v_j(j) = 1 implied),
+// tau[j] their factors; Q (m x k, k = min(m, n)) is formed by applying the
+// reflectors to the first k columns of the identity in reverse order.  The
+// signs are then chosen so that R's diagonal is non-negative (the QR of a
+// full-rank matrix is then unique).
+struct QrClass {
+  int64_t a, q, t;  // class matrix, Q, tau (scratch offsets)
+  int32_t m, n;
+};
+
+__device__ double qr_block_sum(double v, double *red) {
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __syncthreads();  // red may still be read by the previous call
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double t = 0;
+  for (int w = 0; w < nw; w++) t += red[w];
+  return t;
+}
+
+// H_j applied to columns c0 .. c1-1 of X (rows j .. m-1, ld m): warp per column
+__device__ void qr_apply(const double *A, int64_t m, int j, double tau, double *X, int c0, int c1) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const double *v = A + (int64_t)j * m;  // v(j) = 1, v(i > j) = A(i, j)
+  for (int c = c0 + warp; c < c1; c += nw) {
+    double *x = X + (int64_t)c * m;
+    double w = lane == 0 ? x[j] : 0.0;
+    for (int64_t i = j + 1 + lane; i < m; i += 32) w += v[i] * x[i];
+    for (int o = 16; o; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+    w *= tau;
+    if (lane == 0) x[j] -= w;
+    for (int64_t i = j + 1 + lane; i < m; i += 32) x[i] -= w * v[i];
+  }
+}
+
+__global__ void __launch_bounds__(512) qr_householder_kernel(const QrClass *cls, double *scr) {
+  const QrClass C = cls[blockIdx.x];
+  double *A = scr + C.a, *Q = scr + C.q, *tau = scr + C.t;
+  const int m = C.m, n = C.n, k = m < n ? m : n;
+  __shared__ double red[32];
+  __shared__ double sh_tau, sh_scale;
+  for (int j = 0; j < k; j++) {
+    double *a = A + (int64_t)j * m;
+    double part = 0;
+    for (int64_t i = j + 1 + threadIdx.x; i < m; i += blockDim.x) part += a[i] * a[i];
+    const double below = qr_block_sum(part, red);
+    if (threadIdx.x == 0) {
+      const double alpha = a[j], nrm = sqrt(alpha * alpha + below);
+      if (below == 0.0) {
+        sh_tau = 0.0;  // already zero below the diagonal: H_j = I
+        sh_scale = 0.0;
+      } else {
+        const double beta = alpha >= 0 ? -nrm : nrm;
+        sh_tau = (beta - alpha) / beta;
+        sh_scale = 1.0 / (alpha - beta);
+        a[j] = beta;
+      }
+      tau[j] = sh_tau;
+    }
+    __syncthreads();
+    const double t = sh_tau, sc = sh_scale;
+    if (t != 0.0)
+      for (int64_t i = j + 1 + threadIdx.x; i < m; i += blockDim.x) a[i] *= sc;
+    __syncthreads();
+    if (t != 0.0) qr_apply(A, m, j, t, A, j + 1, n);
+    __syncthreads();
+  }
+  // Q = H_0 ... H_{k-1} I(:, 0:k)
+  for (int64_t e = threadIdx.x; e < (int64_t)m * k; e += blockDim.x)
+    Q[e] = (e % m) == (e / m) ? 1.0 : 0.0;
+  __syncthreads();
+  for (int j = k - 1; j >= 0; j--) {
+    const double t = tau[j];
+    if (t != 0.0) qr_apply(A, m, j, t, Q, j, k);
+    __syncthreads();
+  }
+  // non-negative diagonal of R: flip row i of R and column i of Q together
+  for (int i = threadIdx.x; i < k; i += blockDim.x) tau[i] = A[(int64_t)i * m + i] < 0 ? -1.0 : 1.0;
+  __syncthreads();
+  for (int64_t e = threadIdx.x; e < (int64_t)m * k; e += blockDim.x) Q[e] *= tau[e / m];
+  for (int64_t e = threadIdx.x; e < (int64_t)m * n; e += blockDim.x) {
+    const int64_t i = e % m, c = e / m;
+    if (i < k && i <= c) A[e] *= tau[i];
+  }
+}
+
+// Output scatter of the QR factors: kind 0, a Q block (rows of X x the
+// class's k), element (r, j) = Q(off + r, j); kind 1, an R block (k x columns
+// of Y), element (i, c) = R(i, off + c), zero below the diagonal.
+struct QrOut {
+  int64_t dst, src;  // offset in the output's data; class Q or A in scratch
+  int32_t m, k;      // class rows, bond size
+  int32_t kind, off, len, pad;
+};
+
+__global__ void qr_scatter_kernel(const QrOut *ob, const int64_t *ostart, int64_t nob, int64_t ne,
+                                  const double *scr, double *Qt, double *Rt) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ne) return;
+  int64_t lo = 0, hi = nob - 1;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi + 1) >> 1;
+    if (ostart[mid] <= g) lo = mid; else hi = mid - 1;
+  }
+  const QrOut o = ob[lo];
+  const int64_t e = g - ostart[lo];
+  if (o.kind == 0) {
+    const int64_t r = e % o.len, j = e / o.len;
+    Qt[o.dst + e] = scr[o.src + (o.off + r) + j * (int64_t)o.m];
+  } else {
+    const int64_t i = e % o.k, c = o.off + e / o.k;
+    Rt[o.dst + e] = i <= c ? scr[o.src + i + c * (int64_t)o.m] : 0.0;
+  }
+}
+
+static int64_t box_size(const std::vector<int64_t> &box) {
+  int64_t m = 1;
+  for (size_t k = 0; k < box.size(); k += 2) m *= box[k + 1] - box[k] + 1;
+  return m;
+}
+
+// The row-leg boxes X and column-leg boxes Y of a tensor and the classes they
+// form (connected through blocks; the tensor is block diagonal over them):
+// each class is one dense matrix, its X stacked as rows and its Y as columns
+// in id order.
+struct BoxClasses {
+  std::vector<int32_t> rl, cl;                     // row legs, column legs
+  std::vector<std::vector<int64_t>> xbox, ybox;    // (begin, end) per leg
+  std::vector<int64_t> bx, by;                     // per block: its X and Y
+  std::vector<int64_t> xoff, yoff, xc, yc;         // per X / Y: offset in, and id of, its class
+  std::vector<std::vector<int64_t>> cx, cy;        // per class: its X and Y
+  std::vector<int64_t> M, N;                       // per class: rows and columns
+};
+
+static tq_status box_classes(const tq_bs *T, int32_t n_row_legs, const int64_t *row_legs,
+                             cudaStream_t s, BoxClasses &K) {
+  const int32_t r = T->rank;
+  std::vector<bool> used(r, false);
+  for (int32_t q = 0; q < n_row_legs; q++) {
+    if (row_legs[q] < 0 || row_legs[q] >= r || used[row_legs[q]])
+      return fail(TQ_ERR_INVALID, "row legs out of range or repeated");
+    used[row_legs[q]] = true;
+    K.rl.push_back((int32_t)row_legs[q]);
+  }
+  for (int32_t l = 0; l < r; l++)
+    if (!used[l]) K.cl.push_back(l);
+  tq_bs *tm = const_cast<tq_bs *>(T);
+  TQ_CHECK(sync_host_meta(tm, s));
+  TQ_CHECK(sync_device_meta(tm, s));
+  const int64_t nb = T->nb;
+  // row / column boxes -> ids; intervals per leg must be equal or disjoint
+  for (int32_t l = 0; l < r; l++) {
+    std::vector<std::pair<int64_t, int64_t>> iv;
+    for (int64_t b = 0; b < nb; b++) iv.push_back({T->h_begin[b * r + l], T->h_end[b * r + l]});
+    std::sort(iv.begin(), iv.end());
+    for (size_t k = 1; k < iv.size(); k++)
+      if (iv[k] != iv[k - 1] && iv[k].first <= iv[k - 1].second)
+        return fail(TQ_ERR_UNSUPPORTED, "the factorisations need sector boxes: intervals of a "
+                                        "leg must be equal or disjoint");
+  }
+  std::map<std::vector<int64_t>, int64_t> xid, yid;
+  K.bx.resize(nb);
+  K.by.resize(nb);
+  for (int64_t b = 0; b < nb; b++) {
+    std::vector<int64_t> kx, ky;
+    for (int32_t l : K.rl) kx.push_back(T->h_begin[b * r + l]), kx.push_back(T->h_end[b * r + l]);
+    for (int32_t l : K.cl) ky.push_back(T->h_begin[b * r + l]), ky.push_back(T->h_end[b * r + l]);
+    auto fx = xid.emplace(kx, (int64_t)K.xbox.size());
+    if (fx.second) K.xbox.push_back(kx);
+    auto fy = yid.emplace(ky, (int64_t)K.ybox.size());
+    if (fy.second) K.ybox.push_back(ky);
+    K.bx[b] = fx.first->second;
+    K.by[b] = fy.first->second;
+  }
+  const int64_t nx = (int64_t)K.xbox.size(), ny = (int64_t)K.ybox.size();
+  // classes: connected components of X and Y through blocks (union-find)
+  std::vector<int64_t> par(nx + ny);
+  std::iota(par.begin(), par.end(), 0);
+  auto find = [&](int64_t a) {
+    while (par[a] != a) a = par[a] = par[par[a]];
+    return a;
+  };
+  for (int64_t b = 0; b < nb; b++) {
+    const int64_t a = find(K.bx[b]), c = find(nx + K.by[b]);
+    if (a != c) par[std::max(a, c)] = std::min(a, c);
+  }
+  std::map<int64_t, int64_t> cid;
+  K.xoff.assign(nx, 0);
+  K.yoff.assign(ny, 0);
+  K.xc.assign(nx, -1);
+  K.yc.assign(ny, -1);
+  for (int64_t x = 0; x < nx; x++) {
+    auto f = cid.emplace(find(x), (int64_t)K.cx.size());
+    if (f.second) K.cx.emplace_back(), K.cy.emplace_back(), K.M.push_back(0), K.N.push_back(0);
+    const int64_t c = f.first->second;
+    K.xc[x] = c;
+    K.xoff[x] = K.M[c];
+    K.M[c] += box_size(K.xbox[x]);
+    K.cx[c].push_back(x);
+  }
+  for (int64_t y = 0; y < ny; y++) {
+    const int64_t c = cid.at(find(nx + y));
+    K.yc[y] = c;
+    K.yoff[y] = K.N[c];
+    K.N[c] += box_size(K.ybox[y]);
+    K.cy[c].push_back(y);
+  }
+  return TQ_OK;
+}
 }  // namespace tq
 
 using namespace tq;
@@ -215,82 +428,15 @@ extern "C" tq_status tq_bs_svd(const tq_bs *T, int32_t n_row_legs, const int64_t
     return fail(TQ_ERR_INVALID, "need at least one row leg and one column leg");
   if (r + 1 > TQ_MAXR) return fail(TQ_ERR_UNSUPPORTED, "rank above 11");
   if (!(cutoff >= 0.0)) return fail(TQ_ERR_INVALID, "cutoff must be non-negative");
-  std::vector<int32_t> rl, cl;
-  std::vector<bool> used(r, false);
-  for (int32_t q = 0; q < n_row_legs; q++) {
-    if (row_legs[q] < 0 || row_legs[q] >= r || used[row_legs[q]])
-      return fail(TQ_ERR_INVALID, "row legs out of range or repeated");
-    used[row_legs[q]] = true;
-    rl.push_back((int32_t)row_legs[q]);
-  }
-  for (int32_t l = 0; l < r; l++)
-    if (!used[l]) cl.push_back(l);
   cudaStream_t s = (cudaStream_t)stream;
-  tq_bs *tm = const_cast<tq_bs *>(T);
-  TQ_CHECK(sync_host_meta(tm, s));
-  TQ_CHECK(sync_device_meta(tm, s));
+  BoxClasses K;
+  TQ_CHECK(box_classes(T, n_row_legs, row_legs, s, K));
+  const std::vector<int32_t> &rl = K.rl, &cl = K.cl;
+  const std::vector<std::vector<int64_t>> &xbox = K.xbox, &ybox = K.ybox, &cx = K.cx, &cy = K.cy;
+  const std::vector<int64_t> &bx = K.bx, &by = K.by, &xoff = K.xoff, &yoff = K.yoff, &xc = K.xc;
+  const std::vector<int64_t> &M = K.M, &N = K.N;
   const int64_t nb = T->nb;
-  // row / column boxes -> ids; intervals per leg must be equal or disjoint
-  for (int32_t l = 0; l < r; l++) {
-    std::vector<std::pair<int64_t, int64_t>> iv;
-    for (int64_t b = 0; b < nb; b++) iv.push_back({T->h_begin[b * r + l], T->h_end[b * r + l]});
-    std::sort(iv.begin(), iv.end());
-    for (size_t k = 1; k < iv.size(); k++)
-      if (iv[k] != iv[k - 1] && iv[k].first <= iv[k - 1].second)
-        return fail(TQ_ERR_UNSUPPORTED, "the SVD needs sector boxes: intervals of a leg must be "
-                                        "equal or disjoint");
-  }
-  std::map<std::vector<int64_t>, int64_t> xid, yid;
-  std::vector<int64_t> bx(nb), by(nb);
-  std::vector<std::vector<int64_t>> xbox, ybox;
-  for (int64_t b = 0; b < nb; b++) {
-    std::vector<int64_t> kx, ky;
-    for (int32_t l : rl) kx.push_back(T->h_begin[b * r + l]), kx.push_back(T->h_end[b * r + l]);
-    for (int32_t l : cl) ky.push_back(T->h_begin[b * r + l]), ky.push_back(T->h_end[b * r + l]);
-    auto fx = xid.emplace(kx, (int64_t)xbox.size());
-    if (fx.second) xbox.push_back(kx);
-    auto fy = yid.emplace(ky, (int64_t)ybox.size());
-    if (fy.second) ybox.push_back(ky);
-    bx[b] = fx.first->second;
-    by[b] = fy.first->second;
-  }
-  const int64_t nx = (int64_t)xbox.size(), ny = (int64_t)ybox.size();
-  // classes: connected components of X and Y through blocks (union-find)
-  std::vector<int64_t> par(nx + ny);
-  std::iota(par.begin(), par.end(), 0);
-  auto find = [&](int64_t a) {
-    while (par[a] != a) a = par[a] = par[par[a]];
-    return a;
-  };
-  for (int64_t b = 0; b < nb; b++) {
-    const int64_t a = find(bx[b]), c = find(nx + by[b]);
-    if (a != c) par[std::max(a, c)] = std::min(a, c);
-  }
-  std::map<int64_t, int64_t> cid;
-  std::vector<std::vector<int64_t>> cx, cy;  // members, in id order
-  std::vector<int64_t> xoff(nx), yoff(ny), xc(nx, -1), yc(ny, -1);
-  auto size_of = [&](const std::vector<int64_t> &box) {
-    int64_t m = 1;
-    for (size_t k = 0; k < box.size(); k += 2) m *= box[k + 1] - box[k] + 1;
-    return m;
-  };
-  std::vector<int64_t> M, N;
-  for (int64_t x = 0; x < nx; x++) {
-    auto f = cid.emplace(find(x), (int64_t)cx.size());
-    if (f.second) cx.emplace_back(), cy.emplace_back(), M.push_back(0), N.push_back(0);
-    const int64_t c = f.first->second;
-    xc[x] = c;
-    xoff[x] = M[c];
-    M[c] += size_of(xbox[x]);
-    cx[c].push_back(x);
-  }
-  for (int64_t y = 0; y < ny; y++) {
-    const int64_t c = cid.at(find(nx + y));
-    yc[y] = c;
-    yoff[y] = N[c];
-    N[c] += size_of(ybox[y]);
-    cy[c].push_back(y);
-  }
+  auto size_of = [](const std::vector<int64_t> &box) { return box_size(box); };
   const int64_t ncls = (int64_t)cx.size();
   // class scratch: matrix (oriented m >= n) then its n x n right factor
   std::vector<SvdClass> cls(ncls);
@@ -469,5 +615,132 @@ extern "C" tq_status tq_bs_svd(const tq_bs *T, int32_t n_row_legs, const int64_t
   *U = gu.release();
   *S = gs.release();
   *V = gv.release();
+  return TQ_OK;
+}
+
+extern "C" tq_status tq_bs_qr(const tq_bs *T, int32_t n_row_legs, const int64_t *row_legs,
+                              tq_stream stream, tq_bs **Qo, tq_bs **Ro) {
+  if (!T || !Qo || !Ro || (n_row_legs > 0 && !row_legs))
+    return fail(TQ_ERR_INVALID, "NULL argument");
+  if (T->dtype != TQ_F64) return fail(TQ_ERR_UNSUPPORTED, "the QR takes float64 tensors");
+  const int32_t r = T->rank;
+  if (n_row_legs < 1 || n_row_legs >= r)
+    return fail(TQ_ERR_INVALID, "need at least one row leg and one column leg");
+  if (r + 1 > TQ_MAXR) return fail(TQ_ERR_UNSUPPORTED, "rank above 11");
+  cudaStream_t s = (cudaStream_t)stream;
+  BoxClasses K;
+  TQ_CHECK(box_classes(T, n_row_legs, row_legs, s, K));
+  const int64_t nb = T->nb, ncls = (int64_t)K.cx.size();
+  std::vector<QrClass> cls(ncls);
+  std::vector<int64_t> kc(ncls), bond_off(ncls);
+  int64_t scr = 0, bond = 0;
+  for (int64_t c = 0; c < ncls; c++) {
+    const int64_t m = K.M[c], n = K.N[c], k = std::min(m, n);
+    if (m > 0x7fffffff || n > 0x7fffffff) return fail(TQ_ERR_UNSUPPORTED, "a class above 2^31 rows");
+    cls[c] = QrClass{scr, scr + m * n, scr + m * n + m * k, (int32_t)m, (int32_t)n};
+    scr += m * n + m * k + k;
+    kc[c] = k;
+    bond_off[c] = bond;
+    bond += k;
+  }
+  std::vector<SvdBlock> sb(nb);
+  std::vector<int64_t> estart(nb);
+  int64_t ne = 0;
+  for (int64_t b = 0; b < nb; b++) {
+    const int64_t c = K.xc[K.bx[b]];
+    sb[b] = SvdBlock{cls[c].a, K.xoff[K.bx[b]], K.yoff[K.by[b]], cls[c].m, 0, 0};
+    estart[b] = ne;
+    int64_t e = 1;
+    for (int32_t l = 0; l < r; l++) e *= T->h_end[b * r + l] - T->h_begin[b * r + l] + 1;
+    ne += e;
+  }
+  DevArray<double> dscr;
+  DevArray<SvdBlock> dsb;
+  DevArray<QrClass> dcls;
+  DevArray<int64_t> dest;
+  DevArray<int32_t> dlegs;
+  TQ_CHECK(dscr.alloc(std::max<int64_t>(scr, 1), s));
+  TQ_CHECK(dsb.alloc(std::max<int64_t>(nb, 1), s));
+  TQ_CHECK(dcls.alloc(std::max<int64_t>(ncls, 1), s));
+  TQ_CHECK(dest.alloc(std::max<int64_t>(nb, 1), s));
+  TQ_CHECK(dlegs.alloc(r, s));
+  std::vector<int32_t> legs(K.rl);
+  legs.insert(legs.end(), K.cl.begin(), K.cl.end());
+  TQ_CUDA(cudaMemsetAsync(dscr.p, 0, std::max<int64_t>(scr, 1) * 8, s));
+  if (nb) {
+    TQ_CUDA(cudaMemcpyAsync(dsb.p, sb.data(), nb * sizeof(SvdBlock), cudaMemcpyHostToDevice, s));
+    TQ_CUDA(cudaMemcpyAsync(dest.p, estart.data(), nb * 8, cudaMemcpyHostToDevice, s));
+  }
+  if (ncls)
+    TQ_CUDA(cudaMemcpyAsync(dcls.p, cls.data(), ncls * sizeof(QrClass), cudaMemcpyHostToDevice, s));
+  TQ_CUDA(cudaMemcpyAsync(dlegs.p, legs.data(), r * 4, cudaMemcpyHostToDevice, s));
+  if (ne)
+    count_launch(), svd_gather_kernel<<<blocks_of(ne), 256, 0, s>>>(
+        T->view(), (int32_t)K.rl.size(), dlegs.p, (int32_t)K.cl.size(), dlegs.p + K.rl.size(),
+        dsb.p, dest.p, ne, dscr.p);
+  if (ncls) count_launch(), qr_householder_kernel<<<(unsigned)ncls, 512, 0, s>>>(dcls.p, dscr.p);
+  TQ_CUDA(cudaGetLastError());
+  // the factors over a new bond leg, one sector of min(M, N) per class
+  std::vector<int64_t> qdim, rdim;
+  for (int32_t l : K.rl) qdim.push_back(T->dimension[l]);
+  qdim.push_back(std::max<int64_t>(bond, 1));
+  rdim.push_back(std::max<int64_t>(bond, 1));
+  for (int32_t l : K.cl) rdim.push_back(T->dimension[l]);
+  std::vector<int64_t> qb, qe, rb, re, ostart;
+  std::vector<QrOut> ob;
+  int64_t nq = 0, nr = 0, oe = 0;
+  for (int64_t c = 0; c < ncls; c++) {
+    if (!kc[c]) continue;
+    for (int64_t x : K.cx[c]) {
+      for (size_t q = 0; q < K.xbox[x].size(); q += 2)
+        qb.push_back(K.xbox[x][q]), qe.push_back(K.xbox[x][q + 1]);
+      qb.push_back(bond_off[c]);
+      qe.push_back(bond_off[c] + kc[c] - 1);
+      const int64_t len = box_size(K.xbox[x]);
+      ob.push_back(QrOut{nq, cls[c].q, cls[c].m, (int32_t)kc[c], 0, (int32_t)K.xoff[x],
+                         (int32_t)len, 0});
+      ostart.push_back(oe);
+      oe += len * kc[c];
+      nq += len * kc[c];
+    }
+  }
+  const int64_t n_qblk = (int64_t)ob.size();
+  for (int64_t c = 0; c < ncls; c++) {
+    if (!kc[c]) continue;
+    for (int64_t y : K.cy[c]) {
+      rb.push_back(bond_off[c]);
+      re.push_back(bond_off[c] + kc[c] - 1);
+      for (size_t q = 0; q < K.ybox[y].size(); q += 2)
+        rb.push_back(K.ybox[y][q]), re.push_back(K.ybox[y][q + 1]);
+      const int64_t len = box_size(K.ybox[y]);
+      ob.push_back(QrOut{nr, cls[c].a, cls[c].m, (int32_t)kc[c], 1, (int32_t)K.yoff[y],
+                         (int32_t)len, 0});
+      ostart.push_back(oe);
+      oe += len * kc[c];
+      nr += len * kc[c];
+    }
+  }
+  const int64_t n_rblk = (int64_t)ob.size() - n_qblk;
+  tq_bs *Qt = nullptr, *Rt = nullptr;
+  TQ_CHECK(tq_bs_create_zeros(TQ_F64, (int32_t)K.rl.size() + 1, qdim.data(), n_qblk, qb.data(),
+                              qe.data(), nullptr, stream, &Qt));
+  std::unique_ptr<tq_bs, tq_status (*)(tq_bs *)> gq(Qt, tq_bs_destroy);
+  TQ_CHECK(tq_bs_create_zeros(TQ_F64, (int32_t)K.cl.size() + 1, rdim.data(), n_rblk, rb.data(),
+                              re.data(), nullptr, stream, &Rt));
+  std::unique_ptr<tq_bs, tq_status (*)(tq_bs *)> gr(Rt, tq_bs_destroy);
+  if (oe) {
+    DevArray<QrOut> dob;
+    DevArray<int64_t> dos;
+    TQ_CHECK(dob.alloc(ob.size(), s));
+    TQ_CHECK(dos.alloc(ostart.size(), s));
+    TQ_CUDA(cudaMemcpyAsync(dob.p, ob.data(), ob.size() * sizeof(QrOut), cudaMemcpyHostToDevice, s));
+    TQ_CUDA(cudaMemcpyAsync(dos.p, ostart.data(), ostart.size() * 8, cudaMemcpyHostToDevice, s));
+    count_launch(), qr_scatter_kernel<<<blocks_of(oe), 256, 0, s>>>(
+        dob.p, dos.p, (int64_t)ob.size(), oe, dscr.p, (double *)Qt->data, (double *)Rt->data);
+    TQ_CUDA(cudaGetLastError());
+  }
+  TQ_CUDA(cudaStreamSynchronize(s));  // host staging dies here
+  *Qo = gq.release();
+  *Ro = gr.release();
   return TQ_OK;
 }
