@@ -61,7 +61,7 @@ typedef enum {
   TQ_PREC_OZAKI = 1,  /* FP64-level: exact integer slices on the bf16 tensor cores */
   TQ_PREC_BF16X3 = 2, /* FP32-level: three-way bf16 split products */
   TQ_PREC_TENSOR = 3  /* half tensors only: fp16 x fp16 products on the tensor cores
-                         (tcgen05 kind::f16), fp32 accumulation, FP64 sums of the
+                         (tcgen05 kind::f16), fp32 accumulation, fp32 sums of the
                          accumulators, one rounding of each result element */
 } tq_precision;
 

@@ -1,6 +1,6 @@
 """Half tensors on the tensor cores (precision "tensor": tcgen05 kind::f16 with
 fp16 A and B, fp32 accumulation in tensor memory, the retired accumulators
-summed in FP64, one rounding of each result element to binary16).
+summed in fp32, one rounding of each result element to binary16).
 
 Against the oracle on the same half-rounded inputs: within 1e-3 of max|C|
 (the result's own rounding is 2^-11) and, element by element, within one

@@ -221,7 +221,8 @@ __global__ void tc_block_stats_kernel(OzSide S, int32_t rt_rows, int32_t slices,
     k *= S.T.end[b * S.T.rank + S.con[q]] - S.T.begin[b * S.T.rank + S.con[q]] + 1;
   rows[b] = m;
   tiles[b] = (m + rt_rows - 1) / rt_rows;
-  units[b] = ((k + 15) / 16) * slices * ((m + 7) / 8);
+  const int64_t kw = oz_kstep_cols(S.f16);
+  units[b] = ((k + kw - 1) / kw) * slices * ((m + 7) / 8);
   mkey[S.key[b]] = m;
 }
 
@@ -231,7 +232,7 @@ __global__ void tc_block_stats_kernel(OzSide S, int32_t rt_rows, int32_t slices,
 // of the native kernel) instead.
 __global__ void tc_out_kernel(DevBS A, DevBS B, LegSpec L, const int32_t *pa, const int32_t *pb,
                               const int64_t *seg, const int64_t *perm, int64_t n_out,
-                              int32_t tile_n, int32_t native_fill, int32_t *nk_pair,
+                              int32_t tile_n, int32_t native_fill, int32_t kw, int32_t *nk_pair,
                               int64_t *tiles, int64_t *ksum, int64_t *nt_native) {
   const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= n_out) return;
@@ -242,8 +243,8 @@ __global__ void tc_out_kernel(DevBS A, DevBS B, LegSpec L, const int32_t *pa, co
     int64_t k = 1;
     for (int q = 0; q < L.nc; q++)
       k *= A.end[i * A.rank + L.al[q]] - A.begin[i * A.rank + L.al[q]] + 1;
-    nk_pair[p] = (int32_t)((k + 15) / 16);
-    tot += (k + 15) / 16;
+    nk_pair[p] = (int32_t)((k + kw - 1) / kw);
+    tot += (k + kw - 1) / kw;
   }
   ksum[o] = tot;
   const int64_t p0 = perm ? perm[seg[o]] : seg[o];
@@ -557,6 +558,7 @@ static tq_status plan_tc_classes(tq_plan *P, int32_t sl, int32_t tn, int64_t nex
   std::vector<OzClassItem> itA, itB;
   std::vector<int32_t> blkA, blkB;
   std::vector<OzClassOut> out((size_t)ncls);
+  const int64_t kw = oz_kstep_cols(A->dtype == TQ_F16);
   std::vector<int64_t> tstart((size_t)ncls + 1, 0), ksum((size_t)ncls);
   std::vector<OzPairRec> prs((size_t)ncls);
   int64_t unitA = 0, unitB = 0, vA = 0, vB = 0;
@@ -567,7 +569,7 @@ static tq_status plan_tc_classes(tq_plan *P, int32_t sl, int32_t tn, int64_t nex
     int64_t ks = 0;
     for (int32_t q = 0; q < nbox; q++) {
       koff[q] = (int32_t)ks;
-      nk[q] = (int32_t)((kbox[bx[q]] + 15) / 16);
+      nk[q] = (int32_t)((kbox[bx[q]] + kw - 1) / kw);
       ks += nk[q];
     }
     if (ks > 0x7fffffff) return TQ_OK;
@@ -704,12 +706,14 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   const tq_bs *A = P->A, *B = P->B;
   int32_t sl = P->opts.slices;
   if (P->opts.precision == TQ_PREC_TENSOR) {
-    // binary16 operands go to the tensor cores as they are: one "slice"
+    // binary16 operands go to the tensor cores as they are, four 16-column
+    // k-steps packed per step
     if (sl > 1) return fail(TQ_ERR_INVALID, "the tensor form has no slices");
-    sl = 1;
+    sl = OZ_F16_PACK;
   }
   if (sl == 0) sl = P->opts.precision == TQ_PREC_OZAKI ? 5 : 3;
-  if (sl < 1 || sl > OZ_MAXS) return fail(TQ_ERR_INVALID, "slice count outside 1..7");
+  if (P->opts.precision != TQ_PREC_TENSOR && (sl < 1 || sl > OZ_MAXS))
+    return fail(TQ_ERR_INVALID, "slice count outside 1..7");
   P->slices = sl;
   const int32_t tn = P->opts.tile_n ? P->opts.tile_n : OZ_N;
   if (tn != 32 && tn != 64 && tn != 96) return fail(TQ_ERR_INVALID, "tile width must be 32, 64 or 96");
@@ -771,6 +775,7 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   TQ_CHECK(P->hyb_tile_start.alloc(no + 1, s));
   count_launch(), tc_out_kernel<<<nblk(no), 256, 0, s>>>(A->view(), B->view(), L, P->pa.p, P->pb.p, P->seg.p,
                                           P->perm.p, no, tn, P->opts.native_fill,
+                                          (int32_t)oz_kstep_cols(A->dtype == TQ_F16),
                                           P->nk_pair.p, tiles.p, P->ksum.p, nt_native.p);
   TQ_CUDA(cudaGetLastError());
   TQ_CHECK(scan_exclusive(tiles.p, P->tc_tile_start.p, no, tot.p + 8, s));

@@ -217,7 +217,8 @@ __device__ __forceinline__ void oz_slice_class(const OzSide &S, int64_t lt) {
   }
   uint8_t *base = S.slices + 256 * it.unit + (int64_t)it.koff * s * G * 256;
   if (S.f16) {
-    for (int64_t q = 0; q < it.nk; q++)
+    // it.nk packed steps of OZ_F16_PACK k-steps; the padding k-steps are zeros
+    for (int64_t q = 0; q < it.nk * OZ_F16_PACK; q++)
       oz_copy_kstep_f16((const __half *)S.T.data, row_ok, ra, op, q, c, G, r,
                         base + q * (int64_t)G * 256);
     return;
@@ -245,7 +246,8 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OzLaunch L) {
   side_operand(S, b, op);
   const int64_t rows = op.rows - rt * rt_rows < rt_rows ? op.rows - rt * rt_rows : rt_rows;
   const int G = (int)((rows + 7) / 8);
-  const int64_t nk = (op.cols + 15) / 16;
+  const int64_t kw = oz_kstep_cols(S.f16);
+  const int64_t nk = (op.cols + kw - 1) / kw;
   uint8_t *base = S.slices + 256 * S.unit_off[b] + nk * (int64_t)s * 256 * (rt_rows / 8) * rt;
   const double *d = (const double *)S.T.data;
   const int r = threadIdx.x >> 1, c = threadIdx.x & 1;
@@ -254,7 +256,7 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OzLaunch L) {
   const bool row_ok = r < rows;
   const int64_t ra = row_ok ? op.base + mixed_addr(grow, op.nr, op.rdim, op.rst) : 0;
   if (S.f16) {
-    for (int64_t q = 0; q < nk; q++)
+    for (int64_t q = 0; q < nk * OZ_F16_PACK; q++)
       oz_copy_kstep_f16((const __half *)S.T.data, row_ok, ra, op, q, c, G, r,
                         base + q * (int64_t)G * 256);
     return;

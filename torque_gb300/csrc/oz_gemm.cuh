@@ -108,6 +108,17 @@ __device__ __forceinline__ void oz_issue(const uint32_t (&col)[OZ_NACC], uint64_
   }
 }
 
+// Binary16 operands: the OZ_F16_PACK k-steps of a packed step, each one MMA
+// (A and B from shared memory) into the one accumulator.
+__device__ __forceinline__ void oz_issue_packed(uint32_t col0, uint64_t da0, uint64_t db0,
+                                                uint32_t a_step, uint32_t b_step, uint32_t idesc,
+                                                uint32_t fresh) {
+#pragma unroll
+  for (int t = 0; t < OZ_F16_PACK; t++)
+    mma_bf16(col0, da0 + (uint64_t)(t * a_step), db0 + (uint64_t)(t * b_step), idesc,
+             (t == 0 && (fresh & 1)) ? 0u : 1u);
+}
+
 template <bool FRESH, int NTM>
 __device__ __forceinline__ void oz_issue_s(int s, const uint32_t (&col)[OZ_NACC], uint64_t da0,
                                            uint64_t db0, uint32_t a_step, uint32_t b_step,
@@ -219,7 +230,7 @@ __device__ __forceinline__ void oz_unpack(const OzLaunch &L, const OzTileRec &r,
 // S > 0: every job of the launch has S slices (straight-line issue code);
 // S = 0: any slice count (dispatched per job); S = OZ_F16: binary16 operands
 // taken as they are (one "slice", kind::f16 with fp16 A and B, fp32
-// accumulation in TMEM, retired accumulators summed in FP64, one rounding of
+// accumulation in TMEM, retired accumulators summed in fp32, one rounding of
 // each result element to binary16).
 constexpr int OZ_F16 = -1;
 
@@ -289,7 +300,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         const OzPairRec *prs = J.prs;
         const uint8_t *sliceA = J.sliceA, *sliceB = J.sliceB;
         const uint32_t ba = (uint32_t)s * T.ga * 256, bb = (uint32_t)s * T.gb * 256;
-        const int n_acc = s < OZ_NACC ? s : OZ_NACC;
+        const int n_acc = S == OZ_F16 ? 1 : s < OZ_NACC ? s : OZ_NACC;
         OzSchedule sch;
         sch.start(T.ksum, n_acc);
         int64_t ev_k;
@@ -380,7 +391,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         oz_unpack(L, cur, T);
         const OzJob &J = *T.J;
         const int s = J.s;
-        const int n_acc = s < OZ_NACC ? s : OZ_NACC;
+        const int n_acc = S == OZ_F16 ? 1 : s < OZ_NACC ? s : OZ_NACC;
         const OzPairRec *prs = J.prs;
         const uint32_t idesc = S == OZ_F16 ? idesc_f16_f32(OZ_M, (uint32_t)T.nmma)
                                            : idesc_bf16_f32(OZ_M, (uint32_t)T.nmma);
@@ -416,9 +427,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
                                                    (uint32_t)T.gb * 16, idesc, fresh,
                                                    tmem + NSLOT * N);
               else if constexpr (S == OZ_F16)
-                oz_issue<1, true, OzSlots<N>::ntm>(col, dA0 + so, dB0 + so, (uint32_t)T.ga * 16,
-                                                   (uint32_t)T.gb * 16, idesc, fresh,
-                                                   tmem + NSLOT * N);
+                oz_issue_packed(col[0], dA0 + so, dB0 + so, (uint32_t)T.ga * 16,
+                                (uint32_t)T.gb * 16, idesc, fresh);
               else
                 oz_issue_s<true, OzSlots<N>::ntm>(s, col, dA0 + so, dB0 + so, (uint32_t)T.ga * 16,
                                                   (uint32_t)T.gb * 16, idesc, fresh,
@@ -469,7 +479,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       OzTile T;
       oz_unpack(L, L.tiles[t], T);
       const OzJob &J = *T.J;
-      const int n_acc = J.s < OZ_NACC ? J.s : OZ_NACC;
+      const int n_acc = S == OZ_F16 ? 1 : J.s < OZ_NACC ? J.s : OZ_NACC;
       const int64_t grow = T.mt * OZ_M + row;
       const bool row_ok = grow < T.m;
       const int er = S != OZ_F16 && row_ok ? J.expA[T.erow + grow] : 0;
@@ -479,8 +489,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       int kb = 0;
       while (kb < 40 && (int64_t(1) << kb) < 16 * T.ksum) kb++;
       const int u = 48 - kb < 32 ? 48 - kb : 32;
-      // binary16 operands: a plain sum of the fp32 accumulators, in FP64
-      std::conditional_t<S == OZ_F16, double, long long> sum[N / 2];
+      // binary16 operands: a plain fp32 sum of the retired fp32 accumulators
+      // (FP64 adds here would outlast the MMAs: GB300's FP64 rate is ~1/60 of
+      // fp32; 2^-24 per fold is far below the result's binary16 rounding)
+      std::conditional_t<S == OZ_F16, float, long long> sum[N / 2];
 #pragma unroll
       for (int y = 0; y < N / 2; y++) sum[y] = 0;
       OzSchedule sch;
@@ -520,7 +532,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
 #pragma unroll
             for (int y = 0; y < 8; y++) {
               if constexpr (S == OZ_F16)
-                sum[8 * x + y] += (double)__uint_as_float(v[x][y]);
+                sum[8 * x + y] += __uint_as_float(v[x][y]);
               else
                 sum[8 * x + y] += (long long)oz_to_int(__uint_as_float(v[x][y]), scale) << shift;
             }
@@ -530,7 +542,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       }
       if (abort_flag) break;
       if constexpr (S == OZ_F16) {
-        // binary16 result: each element rounded once from the FP64 sum
+        // binary16 result: each element rounded once from the fp32 sum
         __half *C = (__half *)J.g.C + T.c_off;
         if (J.cls) {
           if (row_ok) {
@@ -541,7 +553,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
               if (gcol < T.n) {
                 const OzRowMap cb = J.rmapB[T.ecol + gcol];
                 C[__ldg(J.offs + ra_.xoff + cb.xi) + ra_.xr + (int64_t)cb.xr * ra_.m] =
-                    __double2half(sum[y]);
+                    __float2half_rn(sum[y]);
               }
             }
           }
@@ -549,7 +561,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
 #pragma unroll
           for (int y = 0; y < N / 2; y++) {
             const int64_t gcol = T.nt * N + cbase + y;
-            if (gcol < T.n) C[grow + gcol * T.m] = __double2half(sum[y]);
+            if (gcol < T.n) C[grow + gcol * T.m] = __float2half_rn(sum[y]);
           }
         }
         continue;

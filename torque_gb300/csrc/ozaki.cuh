@@ -13,8 +13,15 @@ constexpr int OZ_TILE_NS[3] = {32, 64, 96};
 constexpr int OZ_BAND = 8;       // row tiles per band of the tile order
 constexpr int OZ_CHUNK = 21;     // most k-steps of 16 an accumulator holds (K = 336)
 constexpr int OZ_MAXS = 7;       // most slices supported
-constexpr int OZ_MAX_STAGES = 8;
+constexpr int OZ_MAX_STAGES = 32;  // one-slice stages are 7 KB: deep pipelines hide the load latency
 constexpr int OZ_EXP_ZERO = -(1 << 20);  // exponent of an all-zero row
+// Binary16 operands take one product per 16-column k-step; OZ_F16_PACK
+// consecutive k-steps are packed as the "slices" of one wider step (the same
+// bytes in memory), so that one pipeline stage (two bulk copies and two
+// barrier waits) carries that many MMAs: the producer's per-stage cost, not
+// the tensor core, bounded the one-MMA stages.
+constexpr int OZ_F16_PACK = 8;
+__host__ __device__ inline int64_t oz_kstep_cols(bool f16) { return f16 ? 16 * OZ_F16_PACK : 16; }
 
 // Charge-class layout (when the contraction allows it).  Free boxes whose blocks
 // carry the same set of matched contracted boxes form a class; when every pair of
