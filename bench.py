@@ -908,6 +908,15 @@ def e2e(tq, c, ah, bh, kw, steps, ch=None):
     result is compared bit for bit with the same plan's device result."""
     import torch
     an, bn = ah.numpy(), bh.numpy()
+    # the link itself at this moment: torch's own copy of 4 GB of ah
+    nprobe = min(ah.numel(), 1 << 29)
+    probe = torch.empty(nprobe, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    tp = time.perf_counter()
+    probe.copy_(ah[:nprobe], non_blocking=True)
+    torch.cuda.synchronize()
+    link_gbs = 8 * nprobe / (time.perf_counter() - tp) / 1e9
+    del probe
     times, phases = [], []
     same = None
     A = B = None
@@ -946,6 +955,7 @@ def e2e(tq, c, ah, bh, kw, steps, ch=None):
             "h2d_bytes_per_step": 8 * (ah.numel() + bh.numel()),
             "d2h_bytes_per_step": 8 * int(ch.numel()), "steps": steps,
             "host_result_equals_device_result": same,
+            "h2d_link_probe_gbs": link_gbs,
             "path": "tq_bs_set_data(host) x2 + tq_plan_create + tq_plan_execute_to(pinned host "
                     "buffer: the GEMM writes the result over the host link as it runs)"}
 
