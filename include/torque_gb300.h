@@ -116,6 +116,12 @@ tq_status tq_bs_create_zeros(tq_dtype dtype, int32_t rank, const int64_t *dimens
 /* Overwrite all block data (n_elem elements; one for a rank-0 tensor) from
  * host or device memory: DenseTensor::initialize (src/gpu/dense.cuh:172-184). */
 tq_status tq_bs_set_data(tq_bs *t, const void *data, tq_memkind kind, tq_stream stream);
+/* The same copy, only enqueued on `stream` (no synchronisation): the caller
+ * keeps `data` alive and unchanged until the stream has passed the copy.  From
+ * page-locked host memory the copy runs on a copy engine while other streams
+ * compute (a serving loop copies step i+1's inputs during step i's GEMM).  No
+ * reference counterpart. */
+tq_status tq_bs_set_data_async(tq_bs *t, const void *data, tq_memkind kind, tq_stream stream);
 
 /* Copy constructor (block_sparse.cuh:306-327): deep device copy. */
 tq_status tq_bs_clone(const tq_bs *t, tq_stream stream, tq_bs **out);

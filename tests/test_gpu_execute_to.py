@@ -113,3 +113,24 @@ def test_serving_loop_set_data_then_execute_to(tq):
         assert np.array_equal(host.numpy(), Q.result.data())
     with pytest.raises(ValueError):
         A.set_data(np.zeros(3))
+
+
+def test_set_data_async_on_a_copy_stream(tq):
+    """Inputs copied by tq_bs_set_data_async on a side stream from page-locked
+    memory, the compute stream waiting on an event: the result equals the
+    contraction of the new values (and the synchronous form's)."""
+    c = workloads.uneven_u1(peak=12.0, qmax=4)
+    A, B = gpu(tq, c.A, c.a_data), gpu(tq, c.B, c.b_data)
+    rng = np.random.default_rng(22)
+    a2 = torch.from_numpy(rng.standard_normal(c.A.n_elem)).pin_memory()
+    b2 = torch.from_numpy(rng.standard_normal(c.B.n_elem)).pin_memory()
+    side = torch.cuda.Stream()
+    done = torch.cuda.Event()
+    A.set_data(a2.numpy(), stream=side, asynchronous=True)
+    B.set_data(b2.numpy(), stream=side, asynchronous=True)
+    done.record(side)
+    torch.cuda.current_stream().wait_event(done)
+    C = A.contract(B, c.pairs, precision="ozaki", slices=5, layout="reduced")
+    W = gpu(tq, c.A, a2.numpy()).contract(gpu(tq, c.B, b2.numpy()), c.pairs, precision="ozaki",
+                                          slices=5, layout="reduced")
+    assert np.array_equal(C.data(), W.data())

@@ -44,6 +44,7 @@ SIGNATURES = {
     "tq_bs_clone": (ST, [P, P, PP]),
     "tq_bs_create_zeros": (ST, [I32, I32, P64, I64, P64, P64, P64, P, PP]),
     "tq_bs_set_data": (ST, [P, P, I32, P]),
+    "tq_bs_set_data_async": (ST, [P, P, I32, P]),
     "tq_bs_destroy": (ST, [P]),
     "tq_bs_append_blocks": (ST, [P, I64, P64, P64, P64, P, I32, P]),
     "tq_bs_query": (ST, [P, P64, P]),

@@ -194,16 +194,20 @@ class BlockSparseTensor:
                                          None))
         return out
 
-    def set_data(self, source_data, stream=None):
+    def set_data(self, source_data, stream=None, asynchronous=False):
         """Overwrite every element (tq_bs_set_data): a numpy array (host, copied
         before return) or a torch CUDA tensor, n_elem elements of the tensor's
-        dtype in the tensor's layout."""
+        dtype in the tensor's layout.  asynchronous=True only enqueues the copy
+        on `stream` (tq_bs_set_data_async): the source must stay alive and
+        unchanged until the stream has passed it (page-locked host memory then
+        copies while other streams compute)."""
         n = self.n_elem if self.rank else 1
         data, kind = self._data_arg(source_data, self.dtype)
         size = data.numel() if hasattr(data, "numel") else data.size
         if size < n:
             raise ValueError("source holds %d elements; the tensor has %d" % (size, n))
-        check(load().tq_bs_set_data(self._h, self._ptr(data), kind, _stream(stream)))
+        fn = load().tq_bs_set_data_async if asynchronous else load().tq_bs_set_data
+        check(fn(self._h, self._ptr(data), kind, _stream(stream)))
 
     def device_ptr(self) -> int:
         p = ctypes.c_void_p()

@@ -320,6 +320,18 @@ tq_status tq_bs_set_data(tq_bs *t, const void *data, tq_memkind kind, tq_stream 
   return TQ_OK;
 }
 
+tq_status tq_bs_set_data_async(tq_bs *t, const void *data, tq_memkind kind, tq_stream stream) {
+  if (!t) return fail(TQ_ERR_INVALID, "tensor is NULL");
+  if (!data) return fail(TQ_ERR_INVALID, "Source data not allocated!");
+  if (kind != TQ_MEM_HOST && kind != TQ_MEM_DEVICE) return fail(TQ_ERR_INVALID, "bad memory kind");
+  const int64_t n = t->rank == 0 ? 1 : t->n_elem;
+  if (n == 0) return TQ_OK;
+  TQ_CUDA(cudaMemcpyAsync(t->data, data, (size_t)n * dtype_size(t->dtype),
+                          kind == TQ_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                          (cudaStream_t)stream));
+  return TQ_OK;
+}
+
 tq_status tq_bs_clone(const tq_bs *src, tq_stream stream, tq_bs **out) {
   if (!src || !out) return fail(TQ_ERR_INVALID, "NULL argument");
   cudaStream_t s = (cudaStream_t)stream;
