@@ -26,6 +26,7 @@
 #include <type_traits>
 
 #include <cuda_fp16.h>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -283,6 +284,35 @@ class BlockSparseTensor {
                                        q.data(), sz.data(), dir.data(), total, modulus, src,
                                        detail::kind_of(kind), nullptr, &out));
     return BlockSparseTensor(out);
+  }
+
+  // New values for every element (an extension, tq_bs_set_data): n_elem
+  // elements in the tensor's layout, from host or device memory.
+  void set_data(const T *src, cudaMemcpyKind kind = cudaMemcpyHostToDevice) {
+    detail::check(tq_bs_set_data(h_, src, detail::kind_of(kind), nullptr));
+  }
+
+  // Block-level truncated SVD (an extension, float64 tensors; tq_bs_svd):
+  // row_legs against the other legs; U[row legs..., bond], S[bond] and
+  // V[bond, column legs...], keeping at most max_keep values (0: all) above
+  // cutoff times the largest.
+  std::tuple<BlockSparseTensor, BlockSparseTensor, BlockSparseTensor> svd(
+      const arma::uvec &row_legs, long long max_keep = 0, double cutoff = 0.0) const {
+    const auto rl = detail::flat(row_legs);
+    tq_bs *u = nullptr, *s = nullptr, *v = nullptr;
+    detail::check(tq_bs_svd(h_, (int32_t)rl.size(), rl.data(), (int64_t)max_keep, cutoff, nullptr,
+                            &u, &s, &v));
+    return std::make_tuple(BlockSparseTensor(u), BlockSparseTensor(s), BlockSparseTensor(v));
+  }
+
+  // Block-level QR (an extension, float64 tensors; tq_bs_qr): Q[row legs...,
+  // bond] with orthonormal columns and R[bond, column legs...], upper
+  // trapezoidal in each charge class.
+  std::pair<BlockSparseTensor, BlockSparseTensor> qr(const arma::uvec &row_legs) const {
+    const auto rl = detail::flat(row_legs);
+    tq_bs *q = nullptr, *r = nullptr;
+    detail::check(tq_bs_qr(h_, (int32_t)rl.size(), rl.data(), nullptr, &q, &r));
+    return std::make_pair(BlockSparseTensor(q), BlockSparseTensor(r));
   }
 
   // the underlying handle, for calls of the C ABI not wrapped here

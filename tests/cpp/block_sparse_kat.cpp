@@ -2,6 +2,8 @@
 // through the C++ drop-in class torque::gpu::BlockSparseTensor<T>, written the
 // way a reference user writes them, for T = float, double and half (the
 // reference's instantiations, src/gpu/block_sparse.cu:66-148).  Exit status = number of failed checks.
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <vector>
 
@@ -159,10 +161,41 @@ void run_cases() {
   }
 }
 
+// The extensions from C++: a Z2 tensor filled with set_data, its QR
+// reproducing it through contract, and its singular values carrying its
+// Frobenius norm.
+static void factorisations() {
+  using torque::gpu::BlockSparseTensor;
+  std::vector<arma::Col<long long>> q = {{0, 1}, {0, 1}, {0, 1}};
+  std::vector<arma::uvec> sz = {{3, 2}, {2, 4}, {3, 3}};
+  auto t = BlockSparseTensor<double>::from_charges(q, sz, {1, 1, -1}, nullptr, 0, 2);
+  arma::uword n = 0;
+  for (arma::uword k = 0; k < t.block_n_elem.n_elem; k++) n += t.block_n_elem(k);
+  std::vector<double> v(n);
+  for (arma::uword i = 0; i < n; i++) v[i] = std::sin(1.0 + (double)i) + 0.25 * (double)(i % 3);
+  t.set_data(v.data());
+  double norm2 = 0, mx = 0;
+  for (double x : v) norm2 += x * x, mx = std::max(mx, std::fabs(x));
+  auto qr = t.qr(arma::uvec{0, 1});
+  auto back = qr.first.contract(qr.second, arma::umat{{2, 0}});
+  double worst = 0;
+  for (arma::uword i = 0; i < 5; i++)
+    for (arma::uword j = 0; j < 6; j++)
+      for (arma::uword k = 0; k < 6; k++)
+        worst = std::max(worst, std::fabs(back.query({i, j, k}) - t.query({i, j, k})));
+  EXPECT(worst <= 1e-12 * mx);
+  auto svd = t.svd(arma::uvec{0, 1});
+  const BlockSparseTensor<double> &s = std::get<1>(svd);
+  double s2 = 0;
+  for (arma::uword k = 0; k < s.dimension(0); k++) s2 += s.query({k}) * s.query({k});
+  EXPECT(std::fabs(s2 - norm2) <= 1e-12 * norm2);
+}
+
 int main() {
   run_cases<float>();
   run_cases<double>();
   run_cases<__half>();
+  factorisations();
   std::printf("%s (%d failed checks)\n", g_failed ? "FAIL" : "OK", g_failed);
   return g_failed;
 }
