@@ -13,7 +13,7 @@ constexpr int OZ_TILE_NS[3] = {32, 64, 96};
 constexpr int OZ_BAND = 8;       // row tiles per band of the tile order
 constexpr int OZ_CHUNK = 21;     // most k-steps of 16 an accumulator holds (K = 336)
 constexpr int OZ_MAXS = 7;       // most slices supported
-constexpr int OZ_MAX_STAGES = 32;  // one-slice stages are 7 KB: deep pipelines hide the load latency
+constexpr int OZ_MAX_STAGES = 8;
 constexpr int OZ_EXP_ZERO = -(1 << 20);  // exponent of an all-zero row
 // Binary16 operands take one product per 16-column k-step; OZ_F16_PACK
 // consecutive k-steps are packed as the "slices" of one wider step (the same
