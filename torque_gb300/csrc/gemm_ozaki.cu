@@ -95,13 +95,28 @@ __global__ void oz_rowexp_kernel(OzLaunch L) {
   side_operand(S, b, op);
   const double *d = (const double *)S.T.data;
   const int64_t ra = op.base + mixed_addr(r, op.nr, op.rdim, op.rst);
-  unsigned long long mx = 0;
-  for (int64_t c = 0; c < op.cols; c++) {
+  // eight independent loads in flight per iteration (the loop is bound by
+  // load latency, not by arithmetic)
+  unsigned long long m8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int64_t c = 0;
+  for (; c + 8 <= op.cols; c += 8) {
+#pragma unroll
+    for (int x = 0; x < 8; x++) {
+      const unsigned long long bits = (unsigned long long)__double_as_longlong(
+                                          d[ra + mixed_addr(c + x, op.nc, op.cdim, op.cst)]) &
+                                      0x7fffffffffffffffull;
+      m8[x] = bits > m8[x] ? bits : m8[x];
+    }
+  }
+  for (; c < op.cols; c++) {
     const unsigned long long bits =
         (unsigned long long)__double_as_longlong(d[ra + mixed_addr(c, op.nc, op.cdim, op.cst)]) &
         0x7fffffffffffffffull;
-    mx = bits > mx ? bits : mx;
+    m8[0] = bits > m8[0] ? bits : m8[0];
   }
+  unsigned long long mx = 0;
+#pragma unroll
+  for (int x = 0; x < 8; x++) mx = m8[x] > mx ? m8[x] : mx;
   if (mx == 0) return;
   const int e = ilogb(__longlong_as_double((long long)mx)) + 2;
   atomicMax(&S.exps[S.row_off[S.key[b]] + r], e);
@@ -133,11 +148,20 @@ __device__ __forceinline__ long long oz_fixed(double x, int shift) {
   return (b >> 63) ? -(long long)q : (long long)q;
 }
 
-// The s slices of k-step q for one half row (8 columns, c = 0 or 1) of row r of
-// an operand row tile with G row groups, written into the k-step's chunk.
-__device__ __forceinline__ void oz_slice_kstep(const double *d, bool row_ok, int64_t ra,
-                                               const Operand &op, int64_t q, int c, int shift,
-                                               int s, int G, int r, uint8_t *chunk) {
+// The 8 values of half row c (columns q*16 + c*8 ..) of row r (absent ones 0).
+__device__ __forceinline__ void oz_load8(const double *d, bool row_ok, int64_t ra,
+                                         const Operand &op, int64_t q, int c, double (&v)[8]) {
+#pragma unroll
+  for (int x = 0; x < 8; x++) {
+    const int64_t kk = q * 16 + c * 8 + x;
+    v[x] = row_ok && kk < op.cols ? d[ra + mixed_addr(kk, op.nc, op.cdim, op.cst)] : 0.0;
+  }
+}
+
+// The s slices of one half row (its 8 values v) of row r of an operand row
+// tile with G row groups, written into the k-step's chunk.
+__device__ __forceinline__ void oz_slice_kstep(const double (&v)[8], int c, int shift, int s, int G,
+                                               int r, uint8_t *chunk) {
   uint32_t packed[OZ_MAXS][4];
 #pragma unroll
   for (int t = 0; t < OZ_MAXS; t++)
@@ -145,9 +169,7 @@ __device__ __forceinline__ void oz_slice_kstep(const double *d, bool row_ok, int
     for (int w = 0; w < 4; w++) packed[t][w] = 0;
 #pragma unroll
   for (int x = 0; x < 8; x++) {
-    const int64_t kk = q * 16 + c * 8 + x;
-    long long F = 0;
-    if (row_ok && kk < op.cols) F = oz_fixed(d[ra + mixed_addr(kk, op.nc, op.cdim, op.cst)], shift);
+    long long F = oz_fixed(v[x], shift);
     int dig[OZ_MAXS];
 #pragma unroll
     for (int t = OZ_MAXS - 1; t >= 1; t--) {
@@ -173,6 +195,22 @@ __device__ __forceinline__ void oz_slice_kstep(const double *d, bool row_ok, int
     if (t >= s) break;
     uint4 v = make_uint4(packed[t][0], packed[t][1], packed[t][2], packed[t][3]);
     *(uint4 *)(chunk + ((t * G + r / 8) * 2 + c) * 128 + (r % 8) * 16) = v;
+  }
+}
+
+// All nk k-steps of one half row: the loads of k-step q+1 are issued before
+// k-step q is split and stored, so each thread keeps loads in flight.
+__device__ __forceinline__ void oz_slice_rows(const double *d, bool row_ok, int64_t ra,
+                                              const Operand &op, int64_t nk, int c, int shift,
+                                              int s, int G, int r, uint8_t *base) {
+  if (nk <= 0) return;
+  double cur[8], nxt[8];
+  oz_load8(d, row_ok, ra, op, 0, c, cur);
+  for (int64_t q = 0; q < nk; q++) {
+    if (q + 1 < nk) oz_load8(d, row_ok, ra, op, q + 1, c, nxt);
+    oz_slice_kstep(cur, c, shift, s, G, r, base + q * (int64_t)s * G * 256);
+#pragma unroll
+    for (int x = 0; x < 8; x++) cur[x] = nxt[x];
   }
 }
 
@@ -223,9 +261,7 @@ __device__ __forceinline__ void oz_slice_class(const OzSide &S, int64_t lt) {
                         base + q * (int64_t)G * 256);
     return;
   }
-  const double *d = (const double *)S.T.data;
-  for (int64_t q = 0; q < it.nk; q++)
-    oz_slice_kstep(d, row_ok, ra, op, q, c, 8 * s - e, s, G, r, base + q * (int64_t)s * G * 256);
+  oz_slice_rows((const double *)S.T.data, row_ok, ra, op, it.nk, c, 8 * s - e, s, G, r, base);
 }
 
 // One CTA per (side, block, row tile): slices of all k-steps of the tile (or,
@@ -249,7 +285,6 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OzLaunch L) {
   const int64_t kw = oz_kstep_cols(S.f16);
   const int64_t nk = (op.cols + kw - 1) / kw;
   uint8_t *base = S.slices + 256 * S.unit_off[b] + nk * (int64_t)s * 256 * (rt_rows / 8) * rt;
-  const double *d = (const double *)S.T.data;
   const int r = threadIdx.x >> 1, c = threadIdx.x & 1;
   if (r >= G * 8) return;
   const int64_t grow = rt * rt_rows + r;
@@ -262,8 +297,7 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OzLaunch L) {
     return;
   }
   const int e = row_ok ? S.exps[S.row_off[S.key[b]] + grow] : OZ_EXP_ZERO;
-  for (int64_t q = 0; q < nk; q++)
-    oz_slice_kstep(d, row_ok, ra, op, q, c, 8 * s - e, s, G, r, base + q * (int64_t)s * G * 256);
+  oz_slice_rows((const double *)S.T.data, row_ok, ra, op, nk, c, 8 * s - e, s, G, r, base);
 }
 
 // Global tile t of the launch -> its job and (output block, row tile, column tile).
