@@ -221,8 +221,8 @@ __global__ void tc_block_stats_kernel(OzSide S, int32_t rt_rows, int32_t slices,
     k *= S.T.end[b * S.T.rank + S.con[q]] - S.T.begin[b * S.T.rank + S.con[q]] + 1;
   rows[b] = m;
   tiles[b] = (m + rt_rows - 1) / rt_rows;
-  const int64_t kw = oz_kstep_cols(S.f16);
-  units[b] = ((k + kw - 1) / kw) * slices * ((m + 7) / 8);
+  const int64_t kw = oz_kstep_cols(S.f16, S.pack);
+  units[b] = ((k + kw - 1) / kw) * S.pack * slices * ((m + 7) / 8);
   mkey[S.key[b]] = m;
 }
 
@@ -375,6 +375,7 @@ static OzSide make_side(const tq_bs *T, int32_t nfree, const int32_t *fl, int32_
   S.tile_start = tile_start;
   S.unit_off = unit_off;
   S.f16 = T->dtype == TQ_F16;
+  S.pack = 1;  // set with the slice count
   return S;
 }
 
@@ -558,7 +559,9 @@ static tq_status plan_tc_classes(tq_plan *P, int32_t sl, int32_t tn, int64_t nex
   std::vector<OzClassItem> itA, itB;
   std::vector<int32_t> blkA, blkB;
   std::vector<OzClassOut> out((size_t)ncls);
-  const int64_t kw = oz_kstep_cols(A->dtype == TQ_F16);
+  const int32_t pack = oz_pack_of(sl, A->dtype == TQ_F16);
+  const int64_t kw = oz_kstep_cols(A->dtype == TQ_F16, pack);
+  const int64_t se = (int64_t)sl * pack;  // slices per stored step
   std::vector<int64_t> tstart((size_t)ncls + 1, 0), ksum((size_t)ncls);
   std::vector<OzPairRec> prs((size_t)ncls);
   int64_t unitA = 0, unitB = 0, vA = 0, vB = 0;
@@ -591,9 +594,9 @@ static tq_status plan_tc_classes(tq_plan *P, int32_t sl, int32_t tn, int64_t nex
     for (int64_t rt = 0; rt < tmA; rt++) {
       const int32_t rows = (int32_t)std::min<int64_t>(OZ_M, Mc - rt * OZ_M);
       for (int32_t q = 0; q < nbox; q++)
-        itA.push_back(OzClassItem{u0A + rt * ks * sl * (OZ_M / 8), r0 + rt * OZ_M, bbA, koff[q],
+        itA.push_back(OzClassItem{u0A + rt * ks * se * (OZ_M / 8), r0 + rt * OZ_M, bbA, koff[q],
                                   nk[q], rows, q, nbox, 0});
-      unitA += ks * sl * ((rows + 7) / 8);
+      unitA += ks * se * ((rows + 7) / 8);
     }
     // side B: tile-width column tiles
     const int64_t c0 = vB, bbB = (int64_t)blkB.size();
@@ -610,9 +613,9 @@ static tq_status plan_tc_classes(tq_plan *P, int32_t sl, int32_t tn, int64_t nex
     for (int64_t ct = 0; ct < tmB; ct++) {
       const int32_t rows = (int32_t)std::min<int64_t>(tn, Nc - ct * tn);
       for (int32_t q = 0; q < nbox; q++)
-        itB.push_back(OzClassItem{u0B + ct * ks * sl * (tn / 8), c0 + ct * tn, bbB, koff[q],
+        itB.push_back(OzClassItem{u0B + ct * ks * se * (tn / 8), c0 + ct * tn, bbB, koff[q],
                                   nk[q], rows, q, nbox, 0});
-      unitB += ks * sl * ((rows + 7) / 8);
+      unitB += ks * se * ((rows + 7) / 8);
     }
     out[c] = OzClassOut{Mc, Nc, r0, c0};
     tstart[c + 1] = tstart[c] + tmA * tmB;
@@ -653,6 +656,7 @@ static tq_status plan_tc_classes(tq_plan *P, int32_t sl, int32_t tn, int64_t nex
                             P->tilestartA.p, P->unitA.p);
   P->tc_side[1] = make_side(B, L.nfb, L.fb, L.nc, L.bl, P->keyB.p, P->rowB.p, P->rowstartB.p,
                             P->tilestartB.p, P->unitB.p);
+  P->tc_side[0].pack = P->tc_side[1].pack = oz_pack_of(sl, A->dtype == TQ_F16);
   const int64_t n_rows[2] = {P->rowsA, P->rowsB}, n_items[2] = {P->tilesA, P->tilesB},
                 n_exps[2] = {nexpA, nexpB};
   int32_t *exps[2] = {P->expA.p, P->expB.p};
@@ -678,6 +682,7 @@ static tq_status plan_tc_classes(tq_plan *P, int32_t sl, int32_t tn, int64_t nex
   P->out = nullptr;  // a rebuilt job array writes the result tensor's buffer
   J.g = make_gemm_job(P);
   J.f16 = P->A->dtype == TQ_F16;
+  J.pack = oz_pack_of(sl, J.f16);
   J.prs = P->pair_tab.p;
   J.tile_start = P->tc_tile_start.p;
   J.n_tiles = P->tc_tiles;
@@ -744,8 +749,11 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   TQ_CHECK(tB.alloc(B->nb, s));
   TQ_CHECK(uB.alloc(B->nb, s));
   TQ_CHECK(tot.alloc(10, s));
+  const bool f16 = A->dtype == TQ_F16;
+  const int32_t pack = oz_pack_of(sl, f16);
   OzSide SA = make_side(A, L.nfa, L.fa, L.nc, L.al, P->keyA.p, nullptr, nullptr, nullptr, nullptr);
   OzSide SB = make_side(B, L.nfb, L.fb, L.nc, L.bl, P->keyB.p, nullptr, nullptr, nullptr, nullptr);
+  SA.pack = SB.pack = pack;
   count_launch(), tc_block_stats_kernel<<<nblk(A->nb), 256, 0, s>>>(SA, OZ_M, sl, mkA.p, rA.p, tA.p, uA.p);
   count_launch(), tc_block_stats_kernel<<<nblk(B->nb), 256, 0, s>>>(SB, tn, sl, mkB.p, rB.p, tB.p, uB.p);
   TQ_CUDA(cudaGetLastError());
@@ -775,7 +783,7 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   TQ_CHECK(P->hyb_tile_start.alloc(no + 1, s));
   count_launch(), tc_out_kernel<<<nblk(no), 256, 0, s>>>(A->view(), B->view(), L, P->pa.p, P->pb.p, P->seg.p,
                                           P->perm.p, no, tn, P->opts.native_fill,
-                                          (int32_t)oz_kstep_cols(A->dtype == TQ_F16),
+                                          (int32_t)oz_kstep_cols(f16, pack),
                                           P->nk_pair.p, tiles.p, P->ksum.p, nt_native.p);
   TQ_CUDA(cudaGetLastError());
   TQ_CHECK(scan_exclusive(tiles.p, P->tc_tile_start.p, no, tot.p + 8, s));
@@ -812,6 +820,7 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
                             P->tilestartA.p, P->unitA.p);
   P->tc_side[1] = make_side(B, L.nfb, L.fb, L.nc, L.bl, P->keyB.p, P->rowB.p, P->rowstartB.p,
                             P->tilestartB.p, P->unitB.p);
+  P->tc_side[0].pack = P->tc_side[1].pack = oz_pack_of(sl, A->dtype == TQ_F16);
   const int64_t n_rows[2] = {P->rowsA, P->rowsB}, n_tiles[2] = {P->tilesA, P->tilesB},
                 n_exps[2] = {P->nexpA, P->nexpB};
   int32_t *exps[2] = {P->expA.p, P->expB.p};
@@ -830,6 +839,7 @@ static tq_status plan_tc(tq_plan *P, int64_t KA, int64_t KB, cudaStream_t s) {
   P->out = nullptr;  // a rebuilt job array writes the result tensor's buffer
   J.g = make_gemm_job(P);
   J.f16 = P->A->dtype == TQ_F16;
+  J.pack = oz_pack_of(sl, J.f16);
   J.tile_start = P->tc_tile_start.p;
   J.n_tiles = P->tc_tiles;
   J.ksum = P->ksum.p;

@@ -253,7 +253,8 @@ __device__ __forceinline__ void oz_slice_class(const OzSide &S, int64_t lt) {
     ra = op.base + mixed_addr(rm.xr, op.nr, op.rdim, op.rst);
     e = S.exps[vr];
   }
-  uint8_t *base = S.slices + 256 * it.unit + (int64_t)it.koff * s * G * 256;
+  // it.koff and it.nk count stored steps of S.pack k-steps
+  uint8_t *base = S.slices + 256 * it.unit + (int64_t)it.koff * S.pack * s * G * 256;
   if (S.f16) {
     // it.nk packed steps of OZ_F16_PACK k-steps; the padding k-steps are zeros
     for (int64_t q = 0; q < it.nk * OZ_F16_PACK; q++)
@@ -261,7 +262,8 @@ __device__ __forceinline__ void oz_slice_class(const OzSide &S, int64_t lt) {
                         base + q * (int64_t)G * 256);
     return;
   }
-  oz_slice_rows((const double *)S.T.data, row_ok, ra, op, it.nk, c, 8 * s - e, s, G, r, base);
+  oz_slice_rows((const double *)S.T.data, row_ok, ra, op, (int64_t)it.nk * S.pack, c, 8 * s - e, s,
+                G, r, base);
 }
 
 // One CTA per (side, block, row tile): slices of all k-steps of the tile (or,
@@ -282,8 +284,8 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OzLaunch L) {
   side_operand(S, b, op);
   const int64_t rows = op.rows - rt * rt_rows < rt_rows ? op.rows - rt * rt_rows : rt_rows;
   const int G = (int)((rows + 7) / 8);
-  const int64_t kw = oz_kstep_cols(S.f16);
-  const int64_t nk = (op.cols + kw - 1) / kw;
+  const int64_t kw = oz_kstep_cols(S.f16, S.pack);
+  const int64_t nk = (op.cols + kw - 1) / kw * S.pack;  // 16-column k-steps (zero past cols)
   uint8_t *base = S.slices + 256 * S.unit_off[b] + nk * (int64_t)s * 256 * (rt_rows / 8) * rt;
   const int r = threadIdx.x >> 1, c = threadIdx.x & 1;
   if (r >= G * 8) return;
@@ -423,7 +425,9 @@ tq_status oz_batch_build(const std::vector<OzJob> &jobs, const std::vector<OzSid
     if (jobs[j].f16 != f16)
       return fail(TQ_ERR_UNSUPPORTED, "binary16 and float64 jobs cannot share a tensor-core launch");
     jt[j + 1] = jt[j] + jobs[j].n_tiles;
-    s_max = jobs[j].s > s_max ? jobs[j].s : s_max;
+    // a stage holds one stored step: s slices of `pack` k-steps
+    const int se_j = jobs[j].s * (jobs[j].pack > 0 ? jobs[j].pack : 1);
+    s_max = se_j > s_max ? se_j : s_max;
     if (jobs[j].tile_n != tile_n)
       return fail(TQ_ERR_INVALID, "the jobs of one tensor-core launch must share the tile width");
   }
@@ -459,9 +463,9 @@ tq_status oz_batch_build(const std::vector<OzJob> &jobs, const std::vector<OzSid
   L.n_slice_tiles = stl[ns];
   L.n_exps = se[ns];
   L.s_max = s_max;
-  L.s_all = s_max;
+  L.s_all = nj ? jobs[0].s : 0;
   for (int64_t j = 0; j < nj; j++)
-    if (jobs[j].s != s_max) L.s_all = 0;
+    if (jobs[j].s != L.s_all || jobs[j].pack != oz_pack_of(jobs[j].s, jobs[j].f16)) L.s_all = 0;
   L.tile_n = tile_n;
   L.f16 = f16;
   L.nstages = oz_stages(s_max, tile_n);

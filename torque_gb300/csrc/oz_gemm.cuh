@@ -18,7 +18,7 @@ constexpr int OZ_THREADS = 320;  // warp 0: loads, warp 1: MMA, warps 2-9: epilo
 constexpr uint32_t OZ_TMEM_COLS = 512;
 // TMEM: OZ_NACC + 1 slots of tile-width columns (at most 480 of 512)
 constexpr int OZ_NACC = 4;
-constexpr int OZ_SMEM_BYTES = 200 * 1024;
+constexpr int OZ_SMEM_BYTES = 216 * 1024;  // three two-k-step stages of five slices
 
 // ---------------------------------------------------------------- conversion
 // T * 2^e as a correctly rounded double, integer operations only (the rare
@@ -141,11 +141,15 @@ struct OzSchedule {
   int64_t next[OZ_NACC];
   int64_t ksum;
   int n_acc;
-  __device__ __forceinline__ void start(int64_t ks, int na) {
+  int64_t chunk;
+  // ks (packed) steps; accumulators retire every `pack`-th of OZ_CHUNK steps
+  __device__ __forceinline__ void start(int64_t ks, int na, int pack = 1) {
     ksum = ks;
     n_acc = na;
+    chunk = OZ_CHUNK / pack;
+    const int stag = OZ_STAG / pack;
 #pragma unroll
-    for (int a = 0; a < OZ_NACC; a++) next[a] = OZ_CHUNK - OZ_STAG * a;
+    for (int a = 0; a < OZ_NACC; a++) next[a] = chunk - stag * a;
   }
   // event at or after the current position: (k, kind)
   __device__ __forceinline__ void peek(int64_t &k, int &kind) const {
@@ -159,7 +163,7 @@ struct OzSchedule {
       }
   }
   __device__ __forceinline__ void advance(int kind) {
-    if (kind != OZ_FINAL) next[kind] += OZ_CHUNK;
+    if (kind != OZ_FINAL) next[kind] += chunk;
   }
 };
 
@@ -297,12 +301,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         // job fields in registers: the asm memory clobbers below would reload them
         const OzJob &J = *T.J;
         const int s = J.s;
+        const int pack = S == 5 ? OZ_PACK5 : S != 0 ? 1 : J.pack;
+        const int se = s * pack;  // slices of a stored step
         const OzPairRec *prs = J.prs;
         const uint8_t *sliceA = J.sliceA, *sliceB = J.sliceB;
-        const uint32_t ba = (uint32_t)s * T.ga * 256, bb = (uint32_t)s * T.gb * 256;
+        const uint32_t ba = (uint32_t)se * T.ga * 256, bb = (uint32_t)se * T.gb * 256;
         const int n_acc = S == OZ_F16 ? 1 : s < OZ_NACC ? s : OZ_NACC;
         OzSchedule sch;
-        sch.start(T.ksum, n_acc);
+        sch.start(T.ksum, n_acc, pack);
         int64_t ev_k;
         int ev_kind;
         sch.peek(ev_k, ev_kind);
@@ -314,8 +320,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
           const OzPairRec pr = pn;
           if (sidx + 1 < T.seg1) pn = prs[sidx + 1];
           const int64_t nk = pr.nk;
-          const uint8_t *ga = sliceA + pr.a_off + nk * s * 256 * (OZ_M / 8) * T.mt;
-          const uint8_t *gb = sliceB + pr.b_off + nk * s * 256 * (N / 8) * T.nt;
+          const uint8_t *ga = sliceA + pr.a_off + nk * se * 256 * (OZ_M / 8) * T.mt;
+          const uint8_t *gb = sliceB + pr.b_off + nk * se * 256 * (N / 8) * T.nt;
           for (int64_t q = 0; q < nk; q++, it++) {
             if (it >= (uint32_t)NS && !mbar_wait(&empty_bar[st], ph, L.wait_ns)) {
               atomicOr(L.err, 1);
@@ -391,12 +397,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         oz_unpack(L, cur, T);
         const OzJob &J = *T.J;
         const int s = J.s;
+        const int pack = S == 5 ? OZ_PACK5 : S != 0 ? 1 : J.pack;
         const int n_acc = S == OZ_F16 ? 1 : s < OZ_NACC ? s : OZ_NACC;
         const OzPairRec *prs = J.prs;
         const uint32_t idesc = S == OZ_F16 ? idesc_f16_f32(OZ_M, (uint32_t)T.nmma)
                                            : idesc_bf16_f32(OZ_M, (uint32_t)T.nmma);
         OzSchedule sch;
-        sch.start(T.ksum, n_acc);
+        sch.start(T.ksum, n_acc, pack);
         int64_t ev_k;
         int ev_kind;
         sch.peek(ev_k, ev_kind);
@@ -422,17 +429,24 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
             tc_fence_after();
             const uint64_t so = (uint64_t)((st * stage_bytes) >> 4);
             if (elect_one()) {
-              if constexpr (S > 0)
-                oz_issue<S, true, OzSlots<N>::ntm>(col, dA0 + so, dB0 + so, (uint32_t)T.ga * 16,
-                                                   (uint32_t)T.gb * 16, idesc, fresh,
-                                                   tmem + NSLOT * N);
-              else if constexpr (S == OZ_F16)
-                oz_issue_packed(col[0], dA0 + so, dB0 + so, (uint32_t)T.ga * 16,
-                                (uint32_t)T.gb * 16, idesc, fresh);
-              else
-                oz_issue_s<true, OzSlots<N>::ntm>(s, col, dA0 + so, dB0 + so, (uint32_t)T.ga * 16,
-                                                  (uint32_t)T.gb * 16, idesc, fresh,
-                                                  tmem + NSLOT * N);
+              // the stage's k-steps one after another: k-step j's slices follow
+              // k-step j-1's; accumulators restart only with the first
+              const uint32_t as = (uint32_t)T.ga * 16, bs = (uint32_t)T.gb * 16;
+              if constexpr (S == OZ_F16) {
+                oz_issue_packed(col[0], dA0 + so, dB0 + so, as, bs, idesc, fresh);
+              } else if constexpr (S > 0) {
+                constexpr int PK = S == 5 ? OZ_PACK5 : 1;
+#pragma unroll
+                for (int j = 0; j < PK; j++)
+                  oz_issue<S, true, OzSlots<N>::ntm>(
+                      col, dA0 + so + (uint64_t)(j * S) * as, dB0 + so + (uint64_t)(j * S) * bs,
+                      as, bs, idesc, j == 0 ? fresh : 0u, tmem + NSLOT * N);
+              } else {
+                for (int j = 0; j < pack; j++)
+                  oz_issue_s<true, OzSlots<N>::ntm>(
+                      s, col, dA0 + so + (uint64_t)(j * s) * as, dB0 + so + (uint64_t)(j * s) * bs,
+                      as, bs, idesc, j == 0 ? fresh : 0u, tmem + NSLOT * N);
+              }
               mma_commit(&empty_bar[st]);
             }
             __syncwarp();
@@ -480,6 +494,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       oz_unpack(L, L.tiles[t], T);
       const OzJob &J = *T.J;
       const int n_acc = S == OZ_F16 ? 1 : J.s < OZ_NACC ? J.s : OZ_NACC;
+      const int pack = S == 5 ? OZ_PACK5 : S != 0 ? 1 : J.pack;
       const int64_t grow = T.mt * OZ_M + row;
       const bool row_ok = grow < T.m;
       const int er = S != OZ_F16 && row_ok ? J.expA[T.erow + grow] : 0;
@@ -487,7 +502,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       // u <= 48 - log2(K) the sum stays below 2^62.1 for any data, and u >= 24
       // keeps D0..D2 (whole multiples of 2^-16) exact.
       int kb = 0;
-      while (kb < 40 && (int64_t(1) << kb) < 16 * T.ksum) kb++;
+      while (kb < 40 && (int64_t(1) << kb) < 16 * pack * T.ksum) kb++;
       const int u = 48 - kb < 32 ? 48 - kb : 32;
       // binary16 operands: a plain fp32 sum of the retired fp32 accumulators
       // (FP64 adds here would outlast the MMAs: GB300's FP64 rate is ~1/60 of
@@ -496,7 +511,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
 #pragma unroll
       for (int y = 0; y < N / 2; y++) sum[y] = 0;
       OzSchedule sch;
-      sch.start(T.ksum, n_acc);
+      sch.start(T.ksum, n_acc, pack);
       bool done = false;
       while (!done && !abort_flag) {
         int64_t ev_k;

@@ -21,7 +21,19 @@ constexpr int OZ_EXP_ZERO = -(1 << 20);  // exponent of an all-zero row
 // barrier waits) carries that many MMAs: the producer's per-stage cost, not
 // the tensor core, bounded the one-MMA stages.
 constexpr int OZ_F16_PACK = 8;
-__host__ __device__ inline int64_t oz_kstep_cols(bool f16) { return f16 ? 16 * OZ_F16_PACK : 16; }
+// Five-slice (FP64-level) jobs carry two 16-column k-steps per pipeline stage
+// (30 MMAs per stage instead of 15: a stage's fixed cost, a barrier round and
+// two bulk copies, is then paid half as often); each accumulator holds at most
+// OZ_CHUNK / OZ_PACK5 packed steps (320 columns, inside the 336-column bound of
+// exact accumulation).
+constexpr int OZ_PACK5 = 2;
+__host__ __device__ inline int32_t oz_pack_of(int32_t s, bool f16) {
+  return f16 ? 1 : (s == 5 ? OZ_PACK5 : 1);
+}
+// columns of K per (packed) step of a job
+__host__ __device__ inline int64_t oz_kstep_cols(bool f16, int32_t pack) {
+  return f16 ? 16 * OZ_F16_PACK : 16 * (int64_t)pack;
+}
 
 // Charge-class layout (when the contraction allows it).  Free boxes whose blocks
 // carry the same set of matched contracted boxes form a class; when every pair of
@@ -72,6 +84,7 @@ struct OzSide {
   int64_t n_rows, n_tiles, n_exps;
   int32_t s, rt_rows;
   int32_t f16;                // binary16 data: copied as they are (one slice, no exponents)
+  int32_t pack;               // 16-column k-steps per stored step (oz_pack_of)
   // class layout (items != NULL): n_tiles counts the items
   const OzClassItem *items;
   const OzRowMap *rmap;       // per virtual row
@@ -101,6 +114,7 @@ struct OzJob {
   int32_t s;
   int32_t tile_n;             // output columns per tile (every job of a launch alike)
   int32_t f16;                // binary16 operands and result, fp32 accumulation (s = 1)
+  int32_t pack;               // 16-column k-steps per pipeline stage (oz_pack_of)
   // class layout (cls != NULL): the GEMM's outputs are the classes, each with one
   // pseudo-pair (its whole contracted range); tile_start and ksum are per class
   const OzClassOut *cls;
