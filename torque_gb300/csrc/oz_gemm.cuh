@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         // job fields in registers: the asm memory clobbers below would reload them
         const OzJob &J = *T.J;
         const int s = J.s;
-        const int pack = S == 5 ? OZ_PACK5 : S != 0 ? 1 : J.pack;
+        const int pack = S == OZ_F16 ? 1 : S > 0 ? oz_pack_for(S) : J.pack;
         const int se = s * pack;  // slices of a stored step
         const OzPairRec *prs = J.prs;
         const uint8_t *sliceA = J.sliceA, *sliceB = J.sliceB;
@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
         oz_unpack(L, cur, T);
         const OzJob &J = *T.J;
         const int s = J.s;
-        const int pack = S == 5 ? OZ_PACK5 : S != 0 ? 1 : J.pack;
+        const int pack = S == OZ_F16 ? 1 : S > 0 ? oz_pack_for(S) : J.pack;
         const int n_acc = S == OZ_F16 ? 1 : s < OZ_NACC ? s : OZ_NACC;
         const OzPairRec *prs = J.prs;
         const uint32_t idesc = S == OZ_F16 ? idesc_f16_f32(OZ_M, (uint32_t)T.nmma)
@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
               if constexpr (S == OZ_F16) {
                 oz_issue_packed(col[0], dA0 + so, dB0 + so, as, bs, idesc, fresh);
               } else if constexpr (S > 0) {
-                constexpr int PK = S == 5 ? OZ_PACK5 : 1;
+                constexpr int PK = oz_pack_for(S);
 #pragma unroll
                 for (int j = 0; j < PK; j++)
                   oz_issue<S, true, OzSlots<N>::ntm>(
@@ -494,7 +494,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(OzLaunch L) {
       oz_unpack(L, L.tiles[t], T);
       const OzJob &J = *T.J;
       const int n_acc = S == OZ_F16 ? 1 : J.s < OZ_NACC ? J.s : OZ_NACC;
-      const int pack = S == 5 ? OZ_PACK5 : S != 0 ? 1 : J.pack;
+      const int pack = S == OZ_F16 ? 1 : S > 0 ? oz_pack_for(S) : J.pack;
       const int64_t grow = T.mt * OZ_M + row;
       const bool row_ok = grow < T.m;
       const int er = S != OZ_F16 && row_ok ? J.expA[T.erow + grow] : 0;

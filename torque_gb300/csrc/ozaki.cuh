@@ -21,14 +21,17 @@ constexpr int OZ_EXP_ZERO = -(1 << 20);  // exponent of an all-zero row
 // barrier waits) carries that many MMAs: the producer's per-stage cost, not
 // the tensor core, bounded the one-MMA stages.
 constexpr int OZ_F16_PACK = 8;
-// Five-slice (FP64-level) jobs carry two 16-column k-steps per pipeline stage
-// (30 MMAs per stage instead of 15: a stage's fixed cost, a barrier round and
-// two bulk copies, is then paid half as often); each accumulator holds at most
-// OZ_CHUNK / OZ_PACK5 packed steps (320 columns, inside the 336-column bound of
-// exact accumulation).
+// Five- and three-slice jobs (the FP64- and FP32-level forms) carry two
+// 16-column k-steps per pipeline stage (30 or 12 MMAs per stage instead of 15
+// or 6: a stage's fixed cost, a barrier round and two bulk copies, is then
+// paid half as often); each accumulator holds at most OZ_CHUNK / 2 packed
+// steps (320 columns, inside the 336-column bound of exact accumulation).
 constexpr int OZ_PACK5 = 2;
+__host__ __device__ constexpr int32_t oz_pack_for(int32_t s) {
+  return s == 5 || s == 3 ? OZ_PACK5 : 1;
+}
 __host__ __device__ inline int32_t oz_pack_of(int32_t s, bool f16) {
-  return f16 ? 1 : (s == 5 ? OZ_PACK5 : 1);
+  return f16 ? 1 : oz_pack_for(s);
 }
 // columns of K per (packed) step of a job
 __host__ __device__ inline int64_t oz_kstep_cols(bool f16, int32_t pack) {
