@@ -172,10 +172,23 @@ def match(A: HostBS, B: HostBS, pairs):
     return pa[:n], pb[:n]
 
 
+class UndefinedRead(IndexError):
+    """Mode 2: the reference CPU path as written would read past the end of a
+    tensor's values; its result is undefined there."""
+
+
+def _raise_mode2(st: int) -> None:
+    if st == 6:
+        raise UndefinedRead("reference CPU path reads past the end of a tensor's values")
+    if st != 0:
+        raise IndexError("reference CPU path indexes a block table column out of range")
+
+
 def contract(A: HostBS, B: HostBS, pairs, mode: int = 0):
     """Reference-layout contraction.  Returns (begin, end, offsets, data) or for a
     rank-0 result the scalar.  mode: 0 accurate, 1 plain double, 2 as-written
-    reference CPU strides (may raise)."""
+    reference CPU strides (raises IndexError where the reference throws, and
+    UndefinedRead where it would read past a tensor's values)."""
     al, bl, nc = _legs(pairs)
     ca, cb = A.c(), B.c()
     L = lib()
@@ -188,8 +201,7 @@ def contract(A: HostBS, B: HostBS, pairs, mode: int = 0):
     data = np.zeros(max(size, 1), np.float64)
     st = L.orc_contract(ctypes.byref(ca), ctypes.byref(cb), nc, _p64(al), _p64(bl), mode,
                         _p64(ob), _p64(oe), _p64(off), _pd(data))
-    if st != 0:
-        raise IndexError("reference CPU path indexes a block table column out of range")
+    _raise_mode2(st)
     if ro == 0:
         return float(data[0])
     return ob[:npairs, :ro], oe[:npairs, :ro], off[:npairs], data[:size]
@@ -223,8 +235,7 @@ def pair_values(A: HostBS, B: HostBS, pairs, i: int, j: int, mode: int = 0, j_bl
     out = np.zeros(m * n, np.float64)
     st = lib().orc_pair_values(ctypes.byref(ca), ctypes.byref(cb), nc, _p64(al), _p64(bl), i, j,
                                j_block, mode, _pd(out))
-    if st != 0:
-        raise IndexError("reference CPU path indexes a block table column out of range")
+    _raise_mode2(st)
     return out.reshape(n, m).T  # column-major m x n
 
 

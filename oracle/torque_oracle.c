@@ -110,6 +110,23 @@ static inline void kadd(ksum *k, double x) {
   k->s = t;
 }
 
+/* Number of values a tensor holds: the end of its furthest block. */
+static int64_t n_values(const orc_bs *T) {
+  int64_t n = 0;
+  for (int64_t b = 0; b < T->n_blocks; b++) {
+    int64_t e = T->offsets[b], c = 1;
+    for (int l = 0; l < T->rank; l++) c *= T->end[b * T->rank + l] - T->begin[b * T->rank + l] + 1;
+    if (e + c > n) n = e + c;
+  }
+  return n;
+}
+
+static int64_t max_of(const int64_t *v, int64_t n) {
+  int64_t m = 0;
+  for (int64_t i = 0; i < n; i++) if (v[i] > m) m = v[i];
+  return m;
+}
+
 int32_t orc_pair_values(const orc_bs *A, const orc_bs *B, int32_t nc,
                         const int64_t *al, const int64_t *bl, int64_t i,
                         int64_t j, int64_t j_block, int32_t mode, double *out) {
@@ -165,6 +182,12 @@ int32_t orc_pair_values(const orc_bs *A, const orc_bs *B, int32_t nc,
     }
     ka[c] = x;
     kb[c] = y;
+  }
+  if (mode == 2 && m > 0 && n > 0 && K > 0 &&
+      (base_a + max_of(ra, m) + max_of(ka, K) >= n_values(A) ||
+       base_b + max_of(rb, n) + max_of(kb, K) >= n_values(B))) {
+    free(ra); free(rb); free(ka); free(kb);
+    return ORC_ERR_READ;
   }
   const double *pa = A->data + base_a, *pb = B->data + base_b;
   for (int64_t c = 0; c < n; c++)

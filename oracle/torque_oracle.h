@@ -41,6 +41,9 @@ typedef struct {
 #define ORC_OK 0
 #define ORC_ERR_INVALID 1
 #define ORC_ERR_RANGE 4
+/* mode 2 only: the as-written strides would read outside the tensor's values,
+ * where the reference's result is undefined. */
+#define ORC_ERR_READ 6
 
 /*
  * Block-pair matching: for every A block (ascending) the B blocks (ascending)
@@ -84,7 +87,10 @@ void orc_pair_boxes(const orc_bs *A, const orc_bs *B, int32_t nc,
  * mode 2: the reference CPU path as written: the element strides come from
  *         column j_block of each tensor's index tables, not the pair's own
  *         blocks (src/tensor/block_sparse.h:531,538).  Returns ORC_ERR_RANGE
- *         when j_block is past a tensor's block count (Armadillo would throw).
+ *         when j_block is past a tensor's block count (Armadillo would throw)
+ *         and ORC_ERR_READ when those strides would address an element past
+ *         the end of a tensor's values (the reference reads there; its
+ *         result is undefined, and the oracle reads nothing).
  * j_block is the position of B block j in A block i's match list.
  */
 int32_t orc_pair_values(const orc_bs *A, const orc_bs *B, int32_t nc,

@@ -1,0 +1,236 @@
+"""The oracle against the reference's own CPU code.
+
+tests/golden/ref_outputs.npz holds outputs of the reference's
+``BlockSparseTensor<double>`` (src/tensor/block_sparse.h, block_sparse.cpp),
+compiled from its sources against the project's Armadillo API subset and run
+by tests/golden/make_ref_outputs.py, in two builds: the headers as they are
+("asis") and with the CPU contract's two stride lookups corrected
+(block_sparse.h:531,538; "fixed").  The fixture tests run everywhere: the
+oracle's reference-layout contraction (mode 0) must give the fixed build's
+block list bit-exactly and its values within 1e-13 of max|C|, and the
+oracle's restatement of the defect (mode 2) must give the as-is build's values
+(or raise where it throws; where the as-is strides would read past a
+tensor's values the reference's result is undefined, the case is marked so
+and the as-is build is not run on it).  Transpositions are bit-exact; overlapping reads
+sum in block order, as the reference does, and are bit-exact too.
+
+The live tests need the compiled reference (oracle/_ref/, present only where
+its sources are) and skip elsewhere: the reference's own known-answer cases
+through the compiled code (which checks the Armadillo API subset), random
+ragged cases against the oracle, the block matcher against orc_match, and a
+regeneration of the fixture compared with the committed one.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, kat_spec, spec_arrays
+from oracle import oracle as orc
+from oracle import ref
+
+if GOLDEN not in sys.path:
+    sys.path.insert(0, GOLDEN)
+import ref_cases as rc  # noqa: E402
+
+TOL = 1e-13
+
+live = pytest.mark.skipif(not (ref.available("fixed") and ref.available("asis")),
+                          reason="the compiled reference (oracle/_ref) exists only where its "
+                                 "sources are")
+
+
+@pytest.fixture(scope="module")
+def fx():
+    return rc.load()
+
+
+def compare_contraction(out, fx, key, sizes_from_fixture=True):
+    """Compare an oracle result with the fixture entries under key."""
+    if key + "scalar" in fx:
+        want = float(fx[key + "scalar"])
+        assert abs(out - want) <= TOL * max(abs(want), 1.0)
+        return
+    ob, oe, off, data = out
+    assert np.array_equal(ob, fx[key + "begin"]) and np.array_equal(oe, fx[key + "end"])
+    assert np.array_equal(off, fx[key + "offsets"])
+    sizes = rc.block_sizes(ob, oe)
+    if key + "values" in fx:
+        want = fx[key + "values"]
+        assert data.shape == want.shape
+        assert np.max(np.abs(data - want)) <= TOL * max(np.max(np.abs(want)), 1e-300)
+    else:
+        got = rc.value_digest(off, sizes, data)
+        assert rc.digest_close(got, fx[key + "digest"], sizes, TOL)
+
+
+@pytest.mark.parametrize("name", list(rc.CONTRACTIONS))
+def test_oracle_matches_reference_outputs(fx, name):
+    A, B, pairs = rc.CONTRACTIONS[name]()
+    assert rc.input_digest(A, B) == str(fx[name + "__input"])
+    assert np.array_equal(pairs, fx[name + "__pairs"])
+    for variant, mode in (("fixed", 0), ("asis", 2)):
+        key = "%s__%s__" % (name, variant)
+        if key + "undefined" in fx:
+            with pytest.raises(orc.UndefinedRead):
+                orc.contract(A, B, pairs, mode=mode)
+            continue
+        if key + "error" in fx:
+            with pytest.raises(IndexError):
+                orc.contract(A, B, pairs, mode=mode)
+            continue
+        compare_contraction(orc.contract(A, B, pairs, mode=mode), fx, key)
+
+
+def test_fixture_covers_both_builds(fx):
+    """The stored cases include the as-is build's wrong values (uneven
+    blocks), its bounds error (more partners than A blocks) and a scalar."""
+    d = fx["u1_85__asis__digest"] - fx["u1_85__fixed__digest"]
+    assert np.max(np.abs(d)) > 1e-3
+    assert "index out of bounds" in str(fx["one_block_many_partners__asis__error"])
+    assert "one_block_many_partners__fixed__values" in fx
+    assert "vector_dot__fixed__scalar" in fx
+
+
+def test_oracle_transpose_matches_reference(fx):
+    T = rc.transpose_r4()
+    assert rc.input_digest(T) == str(fx["transpose_r4__input"])
+    for k, perm in enumerate(rc.TRANSPOSE_PERMS):
+        key = "transpose_r4__%d__" % k
+        assert np.array_equal(fx[key + "perm"], perm)
+        R = orc.hard_transpose(T, perm)
+        assert np.array_equal(R.begin, fx[key + "begin"]) and np.array_equal(R.end, fx[key + "end"])
+        assert np.array_equal(R.strides, fx[key + "tables"])
+        assert np.array_equal(R.offsets, fx[key + "offsets"])
+        assert np.array_equal(R.data, fx[key + "values"])
+
+
+def test_oracle_query_matches_reference(fx):
+    Q, points = rc.query_r3()
+    assert rc.input_digest(Q) == str(fx["query_r3__input"])
+    assert np.array_equal(points, fx["query_r3__points"])
+    got = np.array([orc.query(Q, p) for p in points])
+    assert np.array_equal(got, fx["query_r3__values"])
+    assert np.count_nonzero(got) > 10
+
+
+# ---- live: the compiled reference itself ----------------------------------
+
+def _ref_from_spec(spec, variant):
+    dim, b, e, t, d = spec_arrays(spec)
+    T = ref.RefTensor.empty(dim, variant)
+    o = 0
+    for i in range(b.shape[0]):
+        n = int(np.prod(e[i] - b[i] + 1))
+        table = t[i] if t is not None else np.concatenate([[1], np.cumprod(e[i] - b[i] + 1)[:-1]])
+        T.append_block(d[o:o + n], b[i], e[i], table)
+        o += n
+    return T
+
+
+@live
+@pytest.mark.parametrize("variant", ["fixed", "asis"])
+def test_reference_build_passes_its_known_answers(kat, variant):
+    """The reference's own known answers (test/gpu/block_sparse_test.cu:10-231,
+    the same cases as test/block_sparse_tensor_test.cpp) through the compiled
+    reference: a check of the Armadillo API subset it was compiled against."""
+    for case in kat["cases"]:
+        T = _ref_from_spec(case, variant)
+        for op in case["ops"]:
+            if op[0] == "query":
+                assert T.query(op[1]) == op[2], (case["name"], op)
+            elif op[0] == "modify":
+                T.modify(op[1], op[2])
+            elif op[0] == "append":
+                T.append_block(np.asarray(op[4], np.float64), op[1], op[2], op[3])
+            elif op[0] == "transpose":
+                T = T.hard_transpose(op[1])
+    for case in kat["contractions"]:
+        A = _ref_from_spec(kat_spec(kat, case["A"]), variant)
+        if case["B"] == "A":
+            B = A
+        else:
+            bspec = [c for c in kat["contractions"] if c["name"] == case["B"]][0]["B"] \
+                if isinstance(case["B"], str) else case["B"]
+            B = _ref_from_spec(bspec, variant)
+        C = A.contract(B, case["pairs"])
+        if "scalar" in case:
+            assert C.read()[5][0] == case["scalar"], case["name"]
+            continue
+        for idx, val in case.get("queries", []):
+            assert C.query(idx) == val, (case["name"], idx)
+        if "dense_column_major" in case:
+            H = C.host()
+            got = orc.densify(H).reshape(-1, order="F")
+            assert np.array_equal(got, np.asarray(case["dense_column_major"], np.float64))
+
+
+# No full contraction over two or more legs: the reference's rank-0 path
+# splits the contraction index with the range's dimensions in place of their
+# stride table (block_sparse.h:557-558), which gives a wrong scalar and can
+# read outside the block for ragged ranges; only one-leg scalars are run.
+RANDOM_SHAPES = [([6, 7, 5], [7, 4], [[1, 0]]), ([5, 6, 4], [6, 5, 3], [[1, 0], [0, 1]]),
+                 ([4, 5, 6, 3], [6, 3, 4], [[2, 0], [3, 1]]), ([8], [8, 3], [[0, 0]]),
+                 ([5, 4, 3], [3, 4, 5], [[0, 2], [2, 0]]), ([9], [9], [[0, 0]])]
+
+
+@live
+@pytest.mark.parametrize("seed", range(100, 124))
+def test_live_random_cases_match_oracle(seed):
+    da, db, pairs = RANDOM_SHAPES[seed % len(RANDOM_SHAPES)]
+    A, B, pairs = rc.ragged(seed, da, db, pairs, n_a=6 + seed % 5, n_b=7 + seed % 4)
+    for variant, mode in (("fixed", 0), ("asis", 2)):
+        try:
+            got = orc.contract(A, B, pairs, mode=mode)
+        except orc.UndefinedRead:
+            continue      # the as-is reference would read past its values: not run
+        except IndexError:
+            with pytest.raises(ref.RefError, match="out of bounds"):
+                ref.contract(A, B, pairs, variant=variant)
+            continue
+        want = ref.contract(A, B, pairs, variant=variant)
+        if isinstance(want, float):
+            assert abs(got - want) <= TOL * max(abs(want), 1.0)
+            continue
+        for g, w in zip(got[:3], want[:3]):
+            assert np.array_equal(g, w)
+        assert np.max(np.abs(got[3] - want[3]), initial=0.0) <= \
+            TOL * max(np.max(np.abs(want[3]), initial=0.0), 1e-300)
+
+
+@live
+def test_live_block_matcher_matches_oracle():
+    """block_in_range (block_sparse.cpp:6-175) per A block of the 85-block U(1)
+    pair: the partners, in order, are the oracle's pair list for that block."""
+    A, B, pairs = rc.u1_85()
+    pa, pb = orc.match(A, B, pairs)
+    for i in range(A.n_blocks):
+        found = ref.block_in_range(pairs, A.begin[i], A.end[i], B.begin, B.end)
+        assert np.array_equal(found, pb[pa == i])
+
+
+@live
+def test_live_fixture_is_current(fx):
+    """Regenerating the outputs with the compiled reference gives the
+    committed fixture."""
+    for name, make in rc.CONTRACTIONS.items():
+        A, B, pairs = make()
+        for variant in ("fixed", "asis"):
+            key = "%s__%s__" % (name, variant)
+            if key + "undefined" in fx:
+                continue
+            try:
+                out = ref.contract(A, B, pairs, variant=variant)
+            except ref.RefError as e:
+                assert str(fx[key + "error"]) == str(e)
+                continue
+            if isinstance(out, float):
+                assert float(fx[key + "scalar"]) == out
+                continue
+            assert np.array_equal(out[0], fx[key + "begin"])
+            if key + "values" in fx:
+                assert np.array_equal(out[3], fx[key + "values"])
+            else:
+                d = rc.value_digest(out[2], rc.block_sizes(out[0], out[1]), out[3])
+                assert np.array_equal(d, fx[key + "digest"])
