@@ -234,3 +234,28 @@ def test_live_fixture_is_current(fx):
             else:
                 d = rc.value_digest(out[2], rc.block_sizes(out[0], out[1]), out[3])
                 assert np.array_equal(d, fx[key + "digest"])
+
+
+@live
+@pytest.mark.parametrize("seed", range(200, 206))
+def test_live_transpose_and_query_match_oracle(seed):
+    """Random ragged tensors of rank 2 to 5 (overlapping boxes, extent-1 legs
+    among them): every leg permutation through the reference's
+    hard_transpose (block_sparse.h:607-651) and the oracle's, bit-exact, and
+    64 element reads through its query (block_sparse.h:372-411), bit-exact."""
+    import itertools
+    rng = np.random.default_rng(seed)
+    rank = 2 + seed % 4
+    dims = rng.integers(2, 7, size=rank)
+    T = rc.random_tensor(rng, dims, 6 + seed % 3, max_extent=3)
+    perms = list(itertools.permutations(range(rank)))
+    for p in perms[:: max(1, len(perms) // 12)]:
+        R = ref.hard_transpose(T, p)
+        O = orc.hard_transpose(T, p)
+        assert np.array_equal(R.begin, O.begin) and np.array_equal(R.end, O.end)
+        assert np.array_equal(R.strides, O.strides) and np.array_equal(R.offsets, O.offsets)
+        assert np.array_equal(R.data, O.data)
+    points = np.stack([rng.integers(0, d, 64) for d in dims], 1)
+    R = ref.RefTensor.from_host(T)
+    for p in points:
+        assert R.query(p) == orc.query(T, p)
