@@ -104,19 +104,41 @@ __global__ void check_intervals_kernel(const int64_t *is_begin, const int64_t *i
   begin_of_id[ids[x]] = x;
 }
 
-__global__ void check_disjoint_kernel(const int64_t *begin_of_id, int64_t n_ids,
+// n_ids is read on the device (the scan's total); the grid covers the leg's
+// dimension, an upper bound of it.
+__global__ void check_disjoint_kernel(const int64_t *begin_of_id, const int64_t *n_ids,
                                       const unsigned long long *emax, int32_t *bad) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t + 1 >= n_ids) return;
+  if (t + 1 >= *n_ids) return;
   if ((int64_t)emax[begin_of_id[t]] >= begin_of_id[t + 1]) atomicOr(bad, 1);
 }
 
-__global__ void block_key_kernel(DevBS T, int32_t leg, const int64_t *ids, int64_t radix,
+// state[0] is the running mixed radix (the product of the earlier legs' id counts).
+__global__ void block_key_kernel(DevBS T, int32_t leg, const int64_t *ids, const int64_t *state,
                                  int64_t *key) {
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= T.nb) return;
-  key[b] += ids[T.begin[b * T.rank + leg]] * radix;
+  key[b] += ids[T.begin[b * T.rank + leg]] * state[0];
 }
+
+// After a leg's keys: radix *= max(n_ids, 1), flagging (bad |= 2) a key range
+// beyond 2^62.
+__global__ void radix_step_kernel(const int64_t *n_ids, int64_t *state, int32_t *bad) {
+  const int64_t n = *n_ids > 0 ? *n_ids : 1;
+  if (state[0] > (int64_t(1) << 62) / n) {
+    atomicOr(bad, 2);
+    return;
+  }
+  state[0] *= n;
+}
+
+__global__ void box_keys_init_kernel(int64_t *state, int32_t *bad) {
+  state[0] = 1;
+  state[1] = 0;
+  *bad = 0;
+}
+
+__global__ void box_keys_done_kernel(int64_t *state, const int32_t *bad) { state[1] = *bad; }
 
 __global__ void pair_key_kernel(const int32_t *pa, const int32_t *pb, int64_t n,
                                 const int64_t *ka, const int64_t *kb, int64_t KA, int64_t *key) {
@@ -140,13 +162,19 @@ static inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t -
 
 // Interval-id keys of every block of T over `legs` (mixed radix, first leg
 // fastest).  *K receives the key range; returns UNSUPPORTED if a leg is not
-// laminar or the key range overflows.
+// laminar or the key range overflows.  The radix and the failure flags stay on
+// the device across the legs: one host synchronisation per call.
 static tq_status box_keys(const tq_bs *T, int32_t nlegs, const int32_t *legs, int64_t *key,
                           int64_t *K, cudaStream_t s) {
   TQ_CUDA(cudaMemsetAsync(key, 0, sizeof(int64_t) * std::max<int64_t>(T->nb, 1), s));
-  int64_t radix = 1;
+  *K = 1;
+  if (nlegs == 0) return TQ_OK;
   DevArray<int32_t> bad;
+  DevArray<int64_t> state;  // [radix, flags]
   TQ_CHECK(bad.alloc(1, s));
+  TQ_CHECK(state.alloc(2, s));
+  count_launch(), box_keys_init_kernel<<<1, 1, 0, s>>>(state.p, bad.p);
+  const DevBS v = T->view();
   for (int32_t q = 0; q < nlegs; q++) {
     const int32_t leg = legs[q];
     const int64_t dim = T->dimension[leg];
@@ -161,31 +189,27 @@ static tq_status box_keys(const tq_bs *T, int32_t nlegs, const int32_t *legs, in
     TQ_CUDA(cudaMemsetAsync(is_begin.p, 0, dim * 8, s));
     TQ_CUDA(cudaMemsetAsync(emin.p, 0xff, dim * 8, s));
     TQ_CUDA(cudaMemsetAsync(emax.p, 0, dim * 8, s));
-    TQ_CUDA(cudaMemsetAsync(bad.p, 0, 4, s));
-    const DevBS v = T->view();
     count_launch(), mark_intervals_kernel<<<nblk(T->nb), 256, 0, s>>>(v, leg, is_begin.p, emin.p, emax.p);
     TQ_CHECK(scan_exclusive(is_begin.p, ids.p, dim, total.p, s));
     count_launch(), check_intervals_kernel<<<nblk(dim), 256, 0, s>>>(is_begin.p, ids.p, dim, emin.p, emax.p,
                                                      begin_of_id.p, bad.p);
-    int64_t n_ids = 0;
-    int32_t h_bad = 0;
-    TQ_CUDA(cudaMemcpyAsync(&n_ids, total.p, 8, cudaMemcpyDeviceToHost, s));
-    TQ_CUDA(cudaStreamSynchronize(s));
-    count_launch(), check_disjoint_kernel<<<nblk(std::max<int64_t>(n_ids, 1)), 256, 0, s>>>(begin_of_id.p, n_ids,
-                                                                           emax.p, bad.p);
-    count_launch(), block_key_kernel<<<nblk(T->nb), 256, 0, s>>>(v, leg, ids.p, radix, key);
+    count_launch(), check_disjoint_kernel<<<nblk(std::max<int64_t>(dim, 1)), 256, 0, s>>>(
+        begin_of_id.p, total.p, emax.p, bad.p);
+    count_launch(), block_key_kernel<<<nblk(T->nb), 256, 0, s>>>(v, leg, ids.p, state.p, key);
+    count_launch(), radix_step_kernel<<<1, 1, 0, s>>>(total.p, state.p, bad.p);
     TQ_CUDA(cudaGetLastError());
-    TQ_CUDA(cudaMemcpyAsync(&h_bad, bad.p, 4, cudaMemcpyDeviceToHost, s));
-    TQ_CUDA(cudaStreamSynchronize(s));
-    if (h_bad)
-      return fail(TQ_ERR_UNSUPPORTED,
-                  "reduced layout needs the free legs' intervals to be equal or disjoint "
-                  "(sector boxes); use the reference layout");
-    if (n_ids > 0 && radix > (int64_t(1) << 62) / n_ids)
-      return fail(TQ_ERR_UNSUPPORTED, "output box key range exceeds 2^62");
-    radix *= std::max<int64_t>(n_ids, 1);
   }
-  *K = radix;
+  count_launch(), box_keys_done_kernel<<<1, 1, 0, s>>>(state.p, bad.p);
+  TQ_CUDA(cudaGetLastError());
+  int64_t h[2] = {1, 0};
+  TQ_CUDA(cudaMemcpyAsync(h, state.p, 16, cudaMemcpyDeviceToHost, s));
+  TQ_CUDA(cudaStreamSynchronize(s));
+  if (h[1] & 1)
+    return fail(TQ_ERR_UNSUPPORTED,
+                "reduced layout needs the free legs' intervals to be equal or disjoint "
+                "(sector boxes); use the reference layout");
+  if (h[1] & 2) return fail(TQ_ERR_UNSUPPORTED, "output box key range exceeds 2^62");
+  *K = h[0];
   return TQ_OK;
 }
 
