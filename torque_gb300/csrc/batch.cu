@@ -56,10 +56,17 @@ static void batch_drop_graph(tq_batch *b) {
 static tq_status batch_run(tq_batch *b, cudaStream_t s) {
   for (auto &w : b->waves) {
     for (auto &oz : w->oz) {
-      TQ_CHECK(oz_batch_prepare(*oz, s));
+      {
+        NvtxRange r("tq_prepare");
+        TQ_CHECK(oz_batch_prepare(*oz, s));
+      }
+      NvtxRange r("tq_gemm");
       TQ_CHECK(oz_batch_gemm(*oz, s));
     }
-    for (tq_plan *P : w->hybrid) TQ_CHECK(run_hybrid_native(P, s));
+    for (tq_plan *P : w->hybrid) {
+      NvtxRange r("tq_gemm_native");
+      TQ_CHECK(run_hybrid_native(P, s));
+    }
     for (tq_plan *P : w->others) TQ_CHECK(plan_run(P, s));
   }
   return TQ_OK;

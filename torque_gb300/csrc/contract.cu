@@ -896,8 +896,12 @@ tq_status run_hybrid_native(tq_plan *P, cudaStream_t s) {
 }
 
 static tq_status run_tc(tq_plan *P, cudaStream_t s) {
-  if (P->tc_tiles) TQ_CHECK(oz_batch_prepare(P->tcb, s));
+  if (P->tc_tiles) {
+    NvtxRange r("tq_prepare");
+    TQ_CHECK(oz_batch_prepare(P->tcb, s));
+  }
   if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[1], s));
+  NvtxRange r("tq_gemm");
   if (P->tc_tiles) TQ_CHECK(oz_batch_gemm(P->tcb, s));
   return run_hybrid_native(P, s);
 }
@@ -949,6 +953,7 @@ tq_status validate_legs(const tq_bs *A, const tq_bs *B, int32_t n_legs, const in
 tq_status plan_build(const tq_bs *A, const tq_bs *B, int32_t n_legs, const int64_t *a_legs,
                      const int64_t *b_legs, const tq_contract_opts *opts, cudaStream_t s,
                      tq_plan **plan_out, tq_bs **out, bool structure_only = false) {
+  NvtxRange range("tq_plan");
   LegSpec L;
   TQ_CHECK(validate_legs(A, B, n_legs, a_legs, b_legs, L));
   tq_contract_opts o = {TQ_PREC_NATIVE, TQ_LAYOUT_REFERENCE, 0, 0, 0, 0};
@@ -1158,12 +1163,14 @@ static tq_status plan_run_to(tq_plan *P, void *out, cudaStream_t s) {
   tq_status st = TQ_OK;
   if (P->C->rank == 0) {
     if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[1], s));
+    NvtxRange r("tq_gemm_native");
     st = launch_dot_native(job, P->n_pairs, P->chunk_start.p, P->n_chunks, P->partials.p,
                            P->A->dtype, s);
   } else if (P->tc && P->n_tiles) {
     st = run_tc(P, s);
   } else {
     if (P->profile) TQ_CUDA(cudaEventRecord(P->ev[1], s));
+    NvtxRange r("tq_gemm_native");
     if (P->n_tiles) st = launch_gemm_native(job, P->n_tiles, P->A->dtype, s, &P->nat.w);
   }
   if (st == TQ_OK && P->profile) TQ_CUDA(cudaEventRecord(P->ev[2], s));

@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <algorithm>
@@ -37,6 +38,19 @@ tq_status cuda_fail(cudaError_t e, const char *what);
     tq_status s_ = (call);               \
     if (s_ != TQ_OK) return s_;          \
   } while (0)
+
+// ---------------------------------------------------------------- tracing
+// A named NVTX range over a host scope: the phases of a contraction (plan,
+// operand preparation, GEMM), transposes and batch runs show up on a profiler's
+// timeline, and `ncu --nvtx --nvtx-include "tq_gemm/"` selects the kernels
+// launched inside one.  Ranges are flat (never nested).  Without a tool
+// attached the calls do nothing.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // ---------------------------------------------------------------- memory
 // Stream-ordered device allocation; every call goes through here so that an

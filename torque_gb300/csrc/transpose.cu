@@ -758,6 +758,7 @@ extern "C" tq_status tq_bs_hard_transpose(const tq_bs *t, const int64_t *perm, t
       TQ_CUDA(cudaGetDevice(&dev));
       TQ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
       // a transpose moves bits: the element size picks the kernel
+      NvtxRange range("tq_transpose");
       if (staged) {
         TQ_CHECK(descs.alloc(t->nb, s));
         count_launch(), describe_kernel<<<(unsigned)((t->nb + 255) / 256), 256, 0, s>>>(job, descs.p);
