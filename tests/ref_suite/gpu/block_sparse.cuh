@@ -1,0 +1,10 @@
+// Include-path stand-in for the reference's "gpu/block_sparse.cuh", so that
+// the reference's own GPU test sources compile, unchanged, against the
+// drop-in class.  Like the reference header it brings in cuBLAS's declarations
+// (callers create the handle that contract() takes) and the reference's CPU
+// tensors (its tests use torque::DenseTensor as the expected value).
+#pragma once
+#include <cublas_v2.h>
+
+#include "tensor/block_sparse.h"
+#include "torque_gb300/block_sparse.hpp"

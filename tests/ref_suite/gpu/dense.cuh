@@ -1,0 +1,7 @@
+// Include-path stand-in for the reference's "gpu/dense.cuh" (see
+// block_sparse.cuh beside it): cuBLAS's declarations and the drop-in dense
+// class.
+#pragma once
+#include <cublas_v2.h>
+
+#include "torque_gb300/dense.hpp"
