@@ -171,6 +171,26 @@ int main() {
   CHECK(C(0, 0) == 76.0 && C(1, 0) == 100.0 && C(0, 1) == 103.0 && C(1, 1) == 136.0);
   CHECK(throws_logic([&] { (void)(A * A); }));
 
+  // initializer lists: a flat list is one row, a list of lists gives the rows
+  umat fr({1, 0});
+  CHECK(fr.n_rows == 1 && fr.n_cols == 2 && fr(0, 0) == 1 && fr(0, 1) == 0);
+  umat lr{{1, 0}, {0, 1}, {2, 3}};
+  CHECK(lr.n_rows == 3 && lr.n_cols == 2 && equal(lr, {1, 0, 2, 0, 1, 3}));
+  CHECK(throws_logic([&] { umat bad{{1, 2}, {3}}; }));
+  arma::mat dm{{0, 1}, {2, 3}};
+  CHECK(arma::accu(dm % dm.t()) == 0.0 + 2.0 + 2.0 + 9.0);
+  // unique: distinct elements ascending; shed_row; a column from std::vector
+  CHECK(equal(arma::unique(uvec{3, 1, 3, 2, 1}), {1, 2, 3}));
+  uvec sr{4, 5, 6};
+  sr.shed_row(1);
+  CHECK(equal(sr, {4, 6}));
+  std::vector<uword> stdv{8, 9};
+  uvec fromv(stdv);
+  CHECK(equal(fromv, {8, 9}));
+  // a relation with a plain integer literal
+  CHECK(equal(uvec{0, 2, 0} == 0, {1, 0, 1}));
+  CHECK(equal(arma::find(uvec{0, 2, 0} != 0), {1}));
+
   // copies of large (heap) and small (in-object) vectors are independent
   uvec big(20);
   big[19] = 5;

@@ -1,5 +1,13 @@
-"""The reference's own GPU test sources compile and link, unchanged, against
-the drop-in headers.
+"""The reference's own test sources, unchanged.
+
+CPU suites (test/block_sparse_tensor_test.cpp, dense_tensor_test.cpp,
+sparse_tensor_test.cpp): built from the reference's sources (src/tensor/*.cpp
+and the headers) against the project's Armadillo API subset, with `assert`
+enabled as the reference's default build has it, and run: every assertion
+passes.  This checks the API subset that the oracle build of the reference
+(oracle/build_ref.py) relies on.
+
+GPU suites: they compile and link, unchanged, against the drop-in headers.
 
 test/gpu/block_sparse_test.cu and test/gpu/dense_test.cu of the reference
 include "gpu/block_sparse.cuh" / "gpu/dense.cuh"; tests/ref_suite/ maps those
@@ -60,3 +68,21 @@ def test_reference_gpu_test_builds_against_dropin(tmp_path, catch_main, name):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
     assert os.path.getsize(exe) > 0
+
+
+@pytest.mark.parametrize("name", ["block_sparse_tensor_test", "dense_tensor_test",
+                                  "sparse_tensor_test"])
+def test_reference_cpu_suite_passes(tmp_path, catch_main, name):
+    src = os.path.join(REF, "src")
+    exe = str(tmp_path / name)
+    cmd = ["g++", "-std=c++17", "-O1", "-w", "-I" + os.path.join(ROOT, "oracle", "arma_api"),
+           "-I" + src, "-I" + os.path.join(src, "tensor"),
+           "-I" + os.path.join(REF, "external", "catch2"),
+           os.path.join(REF, "test", name + ".cpp")] + \
+        [os.path.join(src, "tensor", f) for f in ("block_sparse.cpp", "sparse.cpp", "dense.cpp")] + \
+        [catch_main, "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout[-4000:]
+    assert "All tests passed" in out.stdout
