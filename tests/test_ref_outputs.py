@@ -46,7 +46,7 @@ def fx():
     return rc.load()
 
 
-def compare_contraction(out, fx, key, sizes_from_fixture=True):
+def compare_contraction(out, fx, key):
     """Compare an oracle result with the fixture entries under key."""
     if key + "scalar" in fx:
         want = float(fx[key + "scalar"])
