@@ -14,7 +14,8 @@ to 4,096 elements) or the per-block digest of ref_cases.value_digest; a
 scalar result is stored as such, a case where the reference throws stores
 its message, and where the as-is strides would read past a tensor's values
 (the oracle's mode 2 detects it) the as-is build is not run and the case is
-marked "undefined".  Transposition and query cases store their full results.  Keys
+marked "undefined".  Transposition, query and modify cases store their full
+results (for modify: the reads in order and the tensor afterwards).  Keys
 are "<case>__<variant>__<field>"; "<case>__input" is the sha256 of the inputs.
 """
 from __future__ import annotations
@@ -82,6 +83,20 @@ def main() -> None:
     z["query_r3__input"] = np.array(rc.input_digest(Q))
     z["query_r3__points"] = points
     z["query_r3__values"] = np.array([ref.query(Q, p) for p in points])
+    M, ops = rc.modify_r3()
+    z["modify_r3__input"] = np.array(rc.input_digest(M))
+    R = ref.RefTensor.from_host(M)
+    reads = []
+    for kind, idx, value in ops:
+        if kind == "modify":
+            R.modify(idx, value)
+        else:
+            reads.append(R.query(idx))
+    H = R.host()
+    z["modify_r3__reads"] = np.asarray(reads, np.float64)
+    z["modify_r3__begin"], z["modify_r3__end"] = H.begin, H.end
+    z["modify_r3__tables"], z["modify_r3__offsets"], z["modify_r3__values"] = \
+        H.strides, H.offsets, H.data
     np.savez_compressed(rc.FIXTURE, **z)
     print("wrote %s (%d arrays, %d bytes)" % (rc.FIXTURE, len(z), os.path.getsize(rc.FIXTURE)))
 

@@ -112,6 +112,24 @@ def query_r3():
     return T, points
 
 
+def modify_r3():
+    """An overlapping rank-3 tensor and a seeded sequence of element writes and
+    reads: writes inside overlaps (the first block holding the element gets
+    the value, the others zero), outside every block (a nonzero value appends
+    a one-element block, a zero does nothing), and reads after them."""
+    rng = np.random.default_rng(23)
+    T = random_tensor(rng, [5, 6, 4], 7, max_extent=3)
+    ops = []
+    for q in range(48):
+        idx = [int(rng.integers(0, d)) for d in T.dimension]
+        if q % 3 == 2:
+            ops.append(("query", idx, 0.0))
+        else:
+            value = 0.0 if q % 7 == 0 else float(np.round(rng.standard_normal(), 6))
+            ops.append(("modify", idx, value))
+    return T, ops
+
+
 def input_digest(*tensors) -> str:
     h = hashlib.sha256()
     for T in tensors:

@@ -92,3 +92,26 @@ def test_query_matches_reference(tq, fx):
     want = fx["query_r3__values"]
     got = np.array([G.query(p) for p in points])
     assert np.max(np.abs(got - want)) <= 1e-14 * np.max(np.abs(want))
+
+
+def test_modify_matches_reference(tq, fx):
+    """A seeded sequence of element writes and reads on overlapping blocks
+    (block_sparse.h:322-411): the reads, and the tensor afterwards (appended
+    one-element blocks with their all-zero index tables, offsets, values),
+    equal the reference's."""
+    M, ops = rc.modify_r3()
+    assert rc.input_digest(M) == str(fx["modify_r3__input"])
+    G = to_gpu(tq, M)
+    reads = []
+    for kind, idx, value in ops:
+        if kind == "modify":
+            G.modify(idx, value)
+        else:
+            reads.append(G.query(idx))
+    want = fx["modify_r3__reads"]
+    assert np.max(np.abs(np.asarray(reads) - want)) <= 1e-14 * np.max(np.abs(want))
+    dim, b, e, t, o = G.metadata()
+    assert np.array_equal(b.T, fx["modify_r3__begin"]) and np.array_equal(e.T, fx["modify_r3__end"])
+    assert np.array_equal(t.T, fx["modify_r3__tables"])
+    assert np.array_equal(o, fx["modify_r3__offsets"])
+    assert np.array_equal(G.data(), fx["modify_r3__values"])

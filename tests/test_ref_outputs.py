@@ -259,3 +259,24 @@ def test_live_transpose_and_query_match_oracle(seed):
     R = ref.RefTensor.from_host(T)
     for p in points:
         assert R.query(p) == orc.query(T, p)
+
+
+@live
+def test_live_modify_fixture_is_current(fx):
+    """Replaying the write/read sequence on the compiled reference gives the
+    committed reads and final tensor."""
+    M, ops = rc.modify_r3()
+    assert rc.input_digest(M) == str(fx["modify_r3__input"])
+    R = ref.RefTensor.from_host(M)
+    reads = []
+    for kind, idx, value in ops:
+        if kind == "modify":
+            R.modify(idx, value)
+        else:
+            reads.append(R.query(idx))
+    assert np.array_equal(np.asarray(reads), fx["modify_r3__reads"])
+    H = R.host()
+    assert np.array_equal(H.begin, fx["modify_r3__begin"])
+    assert np.array_equal(H.strides, fx["modify_r3__tables"])
+    assert np.array_equal(H.data, fx["modify_r3__values"])
+    assert H.n_blocks > M.n_blocks       # writes outside every block appended blocks
