@@ -110,8 +110,21 @@ class RefTensor:
 
     @classmethod
     def from_host(cls, T: HostBS, variant: str = "fixed") -> "RefTensor":
+        """The constructor from values (column-major blocks); blocks with other
+        index tables are added one by one with append_block, which keeps the
+        given table."""
         if T.n_blocks == 0:
             return cls.empty(T.dimension, variant)
+        dims = T.end - T.begin + 1
+        compact = np.ones_like(dims)
+        if T.rank > 1:
+            compact[:, 1:] = np.cumprod(dims[:, :-1], axis=1)
+        if not np.array_equal(T.strides, compact):
+            t = cls.empty(T.dimension, variant)
+            for b in range(T.n_blocks):
+                o, n = int(T.offsets[b]), int(np.prod(dims[b]))
+                t.append_block(T.data[o:o + n], T.begin[b], T.end[b], T.strides[b])
+            return t
         L = lib(variant)
         dim = np.ascontiguousarray(T.dimension, np.uint64)
         beg = np.ascontiguousarray(T.begin, np.uint64)   # [n_blocks, rank] = rank x n col-major

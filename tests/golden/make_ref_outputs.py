@@ -71,14 +71,15 @@ def main() -> None:
                 z[key + "values"] = data
             else:
                 z[key + "digest"] = rc.value_digest(offsets, rc.block_sizes(begin, end), data)
-    T = rc.transpose_r4()
-    z["transpose_r4__input"] = np.array(rc.input_digest(T))
-    for k, perm in enumerate(rc.TRANSPOSE_PERMS):
-        R = ref.hard_transpose(T, perm)
-        key = "transpose_r4__%d__" % k
-        z[key + "perm"] = np.asarray(perm, np.int64)
-        z[key + "begin"], z[key + "end"] = R.begin, R.end
-        z[key + "tables"], z[key + "offsets"], z[key + "values"] = R.strides, R.offsets, R.data
+    for tname, T in rc.transpose_cases().items():
+        z[tname + "__input"] = np.array(rc.input_digest(T))
+        for k, perm in enumerate(rc.TRANSPOSE_PERMS):
+            R = ref.hard_transpose(T, perm)
+            key = "%s__%d__" % (tname, k)
+            z[key + "perm"] = np.asarray(perm, np.int64)
+            z[key + "begin"], z[key + "end"] = R.begin, R.end
+            z[key + "tables"], z[key + "offsets"], z[key + "values"] = \
+                R.strides, R.offsets, R.data
     Q, points = rc.query_r3()
     z["query_r3__input"] = np.array(rc.input_digest(Q))
     z["query_r3__points"] = points

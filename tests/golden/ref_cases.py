@@ -19,8 +19,13 @@ Cases:
 * ``vector_dot``: rank-1 operands contracted to a scalar;
 * ``one_block_many_partners``: one A block meeting three B blocks; the
   reference as it is reads the index table of A's block 1, 2 and throws;
+* ``custom_tables_r3_k1``: a ragged contraction whose operands store their
+  odd blocks row-major (index tables given to append_block);
 * ``transpose_r4``: leg permutations of a ragged rank-4 tensor whose blocks
   have legs of extent 1 (equal stride-table entries);
+* ``transpose_r4_rowmajor``: the same permutations of a ragged rank-4 tensor
+  whose odd blocks are stored row-major (no extent-1 legs: see below);
+* ``modify_r3``: element writes and reads on overlapping blocks;
 * ``query_r3``: element reads of an overlapping rank-3 tensor (overlaps add).
 """
 from __future__ import annotations
@@ -84,6 +89,7 @@ CONTRACTIONS = {
     "ragged_r4_r2_k2": lambda: ragged(15, [5, 6, 4, 7], [4, 6], [[2, 0], [1, 1]], n_a=9, n_b=6),
     "ragged_r2_r4_k1": lambda: ragged(16, [6, 8], [5, 8, 3, 4], [[1, 1]], n_a=5, n_b=9),
     "vector_dot": lambda: ragged(17, [12], [12], [[0, 0]], n_a=4, n_b=5, max_extent=6),
+    "custom_tables_r3_k1": lambda: custom_tables_case(),
     "one_block_many_partners": lambda: (
         HostBS(np.array([4, 6]), [[0, 0]], [[3, 5]], np.random.default_rng(18).standard_normal(24)),
         HostBS(np.array([6, 3]), [[0, 0], [2, 1], [4, 0]], [[1, 2], [3, 2], [5, 1]],
@@ -105,11 +111,63 @@ def transpose_r4() -> HostBS:
     return HostBS(T.dimension, T.begin, T.end, rng.standard_normal(n))
 
 
+def transpose_r4_rowmajor() -> HostBS:
+    """A ragged rank-4 tensor whose odd blocks are stored row-major.  Every leg
+    of every block has extent 2 or 3: with a leg of extent 1 a row-major
+    index table has two equal entries, and the reference's hard_transpose
+    (block_sparse.h:607-651, through index_to_indices with a sort of the table,
+    space.h:44-59) then gives the extent-1 leg the quotient of its neighbour
+    and writes outside the block."""
+    rng = np.random.default_rng(25)
+    dims = np.array([4, 5, 3, 6], np.int64)
+    nb = 8
+    begin = np.zeros((nb, 4), np.int64)
+    end = np.zeros_like(begin)
+    for b in range(nb):
+        for l, d in enumerate(dims):
+            lo = int(rng.integers(0, d - 1))
+            ext = int(rng.integers(2, min(3, d - lo) + 1))
+            begin[b, l], end[b, l] = lo, lo + ext - 1
+    n = int(np.prod(end - begin + 1, axis=1).sum())
+    return with_custom_tables(HostBS(dims, begin, end, rng.standard_normal(n)))
+
+
+def transpose_cases():
+    """Name -> tensor for the transposition fixtures."""
+    return {"transpose_r4": transpose_r4(), "transpose_r4_rowmajor": transpose_r4_rowmajor()}
+
+
 def query_r3():
     rng = np.random.default_rng(22)
     T = random_tensor(rng, [6, 5, 7], 9, max_extent=4)
     points = np.stack([rng.integers(0, d, 64) for d in T.dimension], 1).astype(np.int64)
     return T, points
+
+
+def with_custom_tables(T: HostBS) -> HostBS:
+    """The same boxes and values with every odd block stored row-major (last
+    leg fastest): index table entries are the products of the later legs'
+    extents, as append_block accepts them."""
+    dims = T.end - T.begin + 1
+    tables = T.strides.copy()
+    data = T.data.copy()
+    for b in range(1, T.n_blocks, 2):
+        d = dims[b]
+        t = np.ones_like(d)
+        for l in range(len(d) - 2, -1, -1):
+            t[l] = t[l + 1] * d[l + 1]
+        tables[b] = t
+        o, n = int(T.offsets[b]), int(np.prod(d))
+        # column-major values -> the same elements in row-major order
+        data[o:o + n] = T.data[o:o + n].reshape(tuple(d[::-1])).transpose().reshape(-1)
+    return HostBS(T.dimension, T.begin, T.end, data, strides=tables, offsets=T.offsets)
+
+
+def custom_tables_case():
+    """A ragged rank-3 x rank-3 contraction over one leg whose operands store
+    their odd blocks row-major."""
+    A, B, pairs = ragged(24, [6, 5, 7], [5, 6, 4], [[1, 0]])
+    return with_custom_tables(A), with_custom_tables(B), pairs
 
 
 def modify_r3():

@@ -35,7 +35,7 @@ def fx():
 
 
 def to_gpu(tq, T):
-    return tq.BlockSparseTensor(T.dimension, T.data, T.begin.T, T.end.T)
+    return tq.BlockSparseTensor(T.dimension, T.data, T.begin.T, T.end.T, T.strides.T)
 
 
 def check(C, fx, key, tol):
@@ -73,11 +73,12 @@ def test_ozaki_matches_reference(tq, fx, name):
     check(C, fx, name + "__fixed__", TOLOZ)
 
 
-def test_transpose_matches_reference(tq, fx):
-    T = rc.transpose_r4()
+@pytest.mark.parametrize("tname", ["transpose_r4", "transpose_r4_rowmajor"])
+def test_transpose_matches_reference(tq, fx, tname):
+    T = rc.transpose_cases()[tname]
     G = to_gpu(tq, T)
     for k, perm in enumerate(rc.TRANSPOSE_PERMS):
-        key = "transpose_r4__%d__" % k
+        key = "%s__%d__" % (tname, k)
         R = G.hard_transpose(perm)
         dim, b, e, t, o = R.metadata()
         assert np.array_equal(b.T, fx[key + "begin"]) and np.array_equal(e.T, fx[key + "end"])

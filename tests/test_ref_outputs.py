@@ -93,11 +93,12 @@ def test_fixture_covers_both_builds(fx):
     assert "vector_dot__fixed__scalar" in fx
 
 
-def test_oracle_transpose_matches_reference(fx):
-    T = rc.transpose_r4()
-    assert rc.input_digest(T) == str(fx["transpose_r4__input"])
+@pytest.mark.parametrize("tname", ["transpose_r4", "transpose_r4_rowmajor"])
+def test_oracle_transpose_matches_reference(fx, tname):
+    T = rc.transpose_cases()[tname]
+    assert rc.input_digest(T) == str(fx[tname + "__input"])
     for k, perm in enumerate(rc.TRANSPOSE_PERMS):
-        key = "transpose_r4__%d__" % k
+        key = "%s__%d__" % (tname, k)
         assert np.array_equal(fx[key + "perm"], perm)
         R = orc.hard_transpose(T, perm)
         assert np.array_equal(R.begin, fx[key + "begin"]) and np.array_equal(R.end, fx[key + "end"])
