@@ -42,7 +42,7 @@ typedef enum {
   TQ_ERR_CUDA = 2,        /* a CUDA runtime call failed */
   TQ_ERR_OOM = 3,         /* device allocation failed (or was refused by the hook) */
   TQ_ERR_RANGE = 4,       /* index outside the tensor */
-  TQ_ERR_UNSUPPORTED = 5, /* valid input outside what this build implements */
+  TQ_ERR_UNSUPPORTED = 5, /* valid input outside what the library implements */
   TQ_ERR_TIMEOUT = 6      /* a bounded device wait gave up */
 } tq_status;
 
