@@ -1,7 +1,7 @@
 """Python access to the reference's own CPU block-sparse tensor (oracle/_ref/).
 
 TEST INFRASTRUCTURE ONLY.  ``build_ref.py`` compiles the reference's
-``BlockSparseTensor<double>`` (src/tensor/block_sparse.h, block_sparse.cpp of
+``BlockSparseTensor<T>``, T double or float (src/tensor/block_sparse.h, block_sparse.cpp of
 Walter-Feng/Torque) against the project's Armadillo API subset, in two
 variants: ``"asis"`` (the headers unchanged) and ``"fixed"`` (the CPU
 contract's two stride lookups corrected, block_sparse.h:531,538).  The
@@ -51,14 +51,14 @@ def lib(variant: str = "fixed"):
         PP = ctypes.POINTER(ctypes.c_void_p)
         L.ref_last_error.restype = ctypes.c_char_p
         L.ref_tensor_new.restype = ctypes.c_int32
-        L.ref_tensor_new.argtypes = [ctypes.c_int32, U, ctypes.c_int64, U, U,
-                                     ctypes.POINTER(ctypes.c_double), PP]
+        L.ref_tensor_new.argtypes = [ctypes.c_int32, ctypes.c_int32, U, ctypes.c_int64, U, U,
+                                     ctypes.c_void_p, PP]
         L.ref_tensor_new_empty.restype = ctypes.c_int32
-        L.ref_tensor_new_empty.argtypes = [ctypes.c_int32, U, PP]
+        L.ref_tensor_new_empty.argtypes = [ctypes.c_int32, ctypes.c_int32, U, PP]
         L.ref_tensor_free.argtypes = [ctypes.c_void_p]
         L.ref_append_block.restype = ctypes.c_int32
-        L.ref_append_block.argtypes = [ctypes.c_void_p, ctypes.c_int32,
-                                       ctypes.POINTER(ctypes.c_double), U, U, U]
+        L.ref_append_block.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, U, U,
+                                       U]
         L.ref_contract.restype = ctypes.c_int32
         L.ref_contract.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, U, PP]
         L.ref_hard_transpose.restype = ctypes.c_int32
@@ -69,10 +69,10 @@ def lib(variant: str = "fixed"):
         L.ref_modify.restype = ctypes.c_int32
         L.ref_modify.argtypes = [ctypes.c_void_p, ctypes.c_int32, U, ctypes.c_double]
         L.ref_tensor_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                      ctypes.POINTER(ctypes.c_int32),
                                       ctypes.POINTER(ctypes.c_int64),
                                       ctypes.POINTER(ctypes.c_int64)]
-        L.ref_tensor_read.argtypes = [ctypes.c_void_p, U, U, U, U, U,
-                                      ctypes.POINTER(ctypes.c_double)]
+        L.ref_tensor_read.argtypes = [ctypes.c_void_p, U, U, U, U, U, ctypes.c_void_p]
         L.ref_block_in_range.restype = ctypes.c_int64
         L.ref_block_in_range.argtypes = [ctypes.c_int32, U, ctypes.c_int32, U, U,
                                          ctypes.c_int32, ctypes.c_int64, U, U, U,
@@ -81,6 +81,11 @@ def lib(variant: str = "fixed"):
         L.ref_product_seconds.restype = ctypes.c_double
         _libs[variant] = L
     return _libs[variant]
+
+
+# element types: the reference's double and float instantiations
+_CODE = {np.dtype(np.float64): 0, np.dtype(np.float32): 1}
+_NP = {0: np.float64, 1: np.float32}
 
 
 def _u(a: np.ndarray):
@@ -98,29 +103,38 @@ class RefTensor:
     def __init__(self, L, handle: ctypes.c_void_p):
         self.L, self.h = L, handle
 
+    @property
+    def dtype(self):
+        dt, r, nb, ne = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64()
+        self.L.ref_tensor_info(self.h, ctypes.byref(dt), ctypes.byref(r), ctypes.byref(nb),
+                               ctypes.byref(ne))
+        return _NP[dt.value]
+
     @classmethod
-    def empty(cls, dimension, variant: str = "fixed") -> "RefTensor":
-        """BlockSparseTensor(dimension): no blocks (a rank-0 tensor holds 0)."""
+    def empty(cls, dimension, variant: str = "fixed", dtype=np.float64) -> "RefTensor":
+        """BlockSparseTensor<T>(dimension): no blocks (a rank-0 tensor holds 0);
+        T is double or float after dtype."""
         L = lib(variant)
         dim = np.ascontiguousarray(dimension, np.uint64).reshape(-1)
         h = ctypes.c_void_p()
-        _check(L, L.ref_tensor_new_empty(dim.size, _u(dim if dim.size else np.zeros(1, np.uint64)),
+        _check(L, L.ref_tensor_new_empty(_CODE[np.dtype(dtype)], dim.size,
+                                         _u(dim if dim.size else np.zeros(1, np.uint64)),
                                          ctypes.byref(h)))
         return cls(L, h)
 
     @classmethod
-    def from_host(cls, T: HostBS, variant: str = "fixed") -> "RefTensor":
-        """The constructor from values (column-major blocks); blocks with other
-        index tables are added one by one with append_block, which keeps the
-        given table."""
+    def from_host(cls, T: HostBS, variant: str = "fixed", dtype=np.float64) -> "RefTensor":
+        """The constructor from values (column-major blocks), the values rounded
+        to dtype (double or float); blocks with other index tables are added
+        one by one with append_block, which keeps the given table."""
         if T.n_blocks == 0:
-            return cls.empty(T.dimension, variant)
+            return cls.empty(T.dimension, variant, dtype)
         dims = T.end - T.begin + 1
         compact = np.ones_like(dims)
         if T.rank > 1:
             compact[:, 1:] = np.cumprod(dims[:, :-1], axis=1)
         if not np.array_equal(T.strides, compact):
-            t = cls.empty(T.dimension, variant)
+            t = cls.empty(T.dimension, variant, dtype)
             for b in range(T.n_blocks):
                 o, n = int(T.offsets[b]), int(np.prod(dims[b]))
                 t.append_block(T.data[o:o + n], T.begin[b], T.end[b], T.strides[b])
@@ -129,10 +143,10 @@ class RefTensor:
         dim = np.ascontiguousarray(T.dimension, np.uint64)
         beg = np.ascontiguousarray(T.begin, np.uint64)   # [n_blocks, rank] = rank x n col-major
         end = np.ascontiguousarray(T.end, np.uint64)
-        data = np.ascontiguousarray(T.data, np.float64)
+        data = np.ascontiguousarray(T.data, dtype)
         h = ctypes.c_void_p()
-        _check(L, L.ref_tensor_new(T.rank, _u(dim), T.n_blocks, _u(beg), _u(end),
-                                   data.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+        _check(L, L.ref_tensor_new(_CODE[np.dtype(dtype)], T.rank, _u(dim), T.n_blocks, _u(beg),
+                                   _u(end), data.ctypes.data_as(ctypes.c_void_p),
                                    ctypes.byref(h)))
         return cls(L, h)
 
@@ -144,17 +158,18 @@ class RefTensor:
     def read(self):
         """(dimension, begin [nb, rank], end, index tables [nb, rank], offsets,
         values); a rank-0 tensor has empty metadata and one value."""
-        rank, nb, ne = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64()
-        self.L.ref_tensor_info(self.h, ctypes.byref(rank), ctypes.byref(nb), ctypes.byref(ne))
+        dt, rank, nb, ne = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64()
+        self.L.ref_tensor_info(self.h, ctypes.byref(dt), ctypes.byref(rank), ctypes.byref(nb),
+                               ctypes.byref(ne))
         r, n = rank.value, nb.value
         dim = np.zeros(max(r, 1), np.uint64)
         beg = np.zeros(max(r * n, 1), np.uint64)
         end = np.zeros_like(beg)
         tab = np.zeros_like(beg)
         off = np.zeros(max(n, 1), np.uint64)
-        data = np.zeros(max(ne.value, 1), np.float64)
+        data = np.zeros(max(ne.value, 1), _NP[dt.value])
         self.L.ref_tensor_read(self.h, _u(dim), _u(beg), _u(end), _u(tab), _u(off),
-                               data.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+                               data.ctypes.data_as(ctypes.c_void_p))
         shape = (n, r)
         return (dim[:r].astype(np.int64), beg[:r * n].reshape(shape).astype(np.int64),
                 end[:r * n].reshape(shape).astype(np.int64),
@@ -162,6 +177,7 @@ class RefTensor:
                 data[:ne.value])
 
     def host(self) -> HostBS:
+        """The tensor as a HostBS (values widened to float64)."""
         dim, beg, end, tab, off, data = self.read()
         return HostBS(dim, beg, end, data, strides=tab, offsets=off)
 
@@ -191,11 +207,10 @@ class RefTensor:
                                          float(number)))
 
     def append_block(self, data, begin, end, table) -> None:
-        d = np.ascontiguousarray(data, np.float64)
+        d = np.ascontiguousarray(data, self.dtype)
         b, e, t = (np.ascontiguousarray(x, np.uint64).reshape(-1) for x in (begin, end, table))
-        _check(self.L, self.L.ref_append_block(
-            self.h, b.size, d.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), _u(b), _u(e),
-            _u(t)))
+        _check(self.L, self.L.ref_append_block(self.h, b.size, d.ctypes.data_as(ctypes.c_void_p),
+                                               _u(b), _u(e), _u(t)))
 
 
 def _legs(pairs) -> np.ndarray:
@@ -203,11 +218,11 @@ def _legs(pairs) -> np.ndarray:
     return np.ascontiguousarray(p.T.reshape(-1))          # n x 2 column-major
 
 
-def contract(A: HostBS, B: HostBS, pairs, variant: str = "fixed"):
-    """The reference's CPU contract.  Returns (begin, end, offsets, values) in
-    the reference layout, or a float for a rank-0 result; raises RefError where
-    the reference throws."""
-    a, b = RefTensor.from_host(A, variant), RefTensor.from_host(B, variant)
+def contract(A: HostBS, B: HostBS, pairs, variant: str = "fixed", dtype=np.float64):
+    """The reference's CPU contract, in double or (dtype float32) float.
+    Returns (begin, end, offsets, values) in the reference layout, or a float
+    for a rank-0 result; raises RefError where the reference throws."""
+    a, b = RefTensor.from_host(A, variant, dtype), RefTensor.from_host(B, variant, dtype)
     dim, beg, end, _, off, data = a.contract(b, pairs).read()
     if dim.size == 0:
         return float(data[0])

@@ -1,10 +1,10 @@
 // C entry points over the reference's own CPU block-sparse tensor
-// (torque::BlockSparseTensor<double>, src/tensor/block_sparse.h:110-656 of
-// Walter-Feng/Torque, with block_in_range from src/tensor/block_sparse.cpp),
-// compiled from the reference's sources against the Armadillo API subset in
-// arma_api/.  TEST INFRASTRUCTURE ONLY: it lets the tests and fixture scripts
-// run the reference's code on the same inputs as the oracle and the CUDA
-// path.  Nothing in the library links it.
+// (torque::BlockSparseTensor<T>, T = double or float,
+// src/tensor/block_sparse.h:110-656 of Walter-Feng/Torque, with block_in_range
+// from src/tensor/block_sparse.cpp), compiled from the reference's sources
+// against the Armadillo API subset in arma_api/.  TEST INFRASTRUCTURE ONLY: it
+// lets the tests and fixture scripts run the reference's code on the same
+// inputs as the oracle and the CUDA path.  Nothing in the library links it.
 //
 // build_ref.py compiles this file twice: once against the reference header as
 // it is, and once with the header's two stride lookups of the CPU contract
@@ -12,10 +12,12 @@
 // header text arrives first in the same translation unit, so the include
 // below is skipped.
 //
-// Metadata crosses the boundary in the reference's own layout: begin and end
-// points are rank x n_blocks column-major (column = block), as arma::umat
-// stores them.  Every call returns 0 on success, 1 when the reference threw
-// its Error type, 2 for any other exception (Armadillo-style bounds errors);
+// A handle carries its element type (REF_F64 or REF_F32); values cross the
+// boundary in that type, scalars (query, modify) as double.  Metadata crosses
+// in the reference's own layout: begin and end points are rank x n_blocks
+// column-major (column = block), as arma::umat stores them.  Every call
+// returns 0 on success, 1 when the reference threw its Error type, 2 for any
+// other exception (Armadillo-style bounds errors, mixed element types);
 // ref_last_error() gives the message.
 #ifndef TORQUE_TENSOR_BLOCK_SPARSE_H
 #include "tensor/block_sparse.h"
@@ -24,16 +26,26 @@
 #include <cstdint>
 #include <cstdlib>
 #include <exception>
+#include <stdexcept>
 #include <string>
+#include <type_traits>
+
+#define REF_F64 0
+#define REF_F32 1
+
+struct ref_tensor {
+  int32_t dtype;
+  void *t;  // torque::BlockSparseTensor<double> or <float>
+};
 
 namespace {
 
-typedef torque::BlockSparseTensor<double> Tensor;
+template <class T> using Tensor = torque::BlockSparseTensor<T>;
 
 // The tensor keeps its values in a protected member; a derived type names it.
-struct DataAccess : Tensor {
-  static double *get(const Tensor &t) { return (t.*(&DataAccess::data)).get(); }
-  static double *release(Tensor &t) { return (t.*(&DataAccess::data)).release(); }
+template <class T> struct DataAccess : Tensor<T> {
+  static T *get(const Tensor<T> &t) { return (t.*(&DataAccess::data)).get(); }
+  static T *release(Tensor<T> &t) { return (t.*(&DataAccess::data)).release(); }
 };
 
 thread_local std::string last_error;
@@ -63,105 +75,63 @@ template <class F> int32_t guarded(F f) {
   }
 }
 
-}  // namespace
-
-extern "C" {
-
-typedef struct ref_tensor ref_tensor;
-
-const char *ref_last_error(void) { return last_error.c_str(); }
-
-// BlockSparseTensor(const T*, begin_points, end_points, total_dimension)
-// (block_sparse.h:155-202).  The tensor copies the values.
-int32_t ref_tensor_new(int32_t rank, const uint64_t *dimension, int64_t n_blocks,
-                       const uint64_t *begin, const uint64_t *end, const double *data,
-                       ref_tensor **out) {
-  return guarded([&] {
-    Tensor *t = new Tensor(data, to_umat(begin, rank, n_blocks), to_umat(end, rank, n_blocks),
-                           to_uvec(dimension, rank));
-    *out = reinterpret_cast<ref_tensor *>(t);
-  });
+template <class T> constexpr int32_t code() {
+  return std::is_same<T, double>::value ? REF_F64 : REF_F32;
 }
 
-// BlockSparseTensor(dimension) (block_sparse.h:147-153): no blocks, one
-// zeroed element (a rank-0 tensor's value).
-int32_t ref_tensor_new_empty(int32_t rank, const uint64_t *dimension, ref_tensor **out) {
-  return guarded([&] {
-    Tensor *t = new Tensor(to_uvec(dimension, rank));
-    *out = reinterpret_cast<ref_tensor *>(t);
-  });
+template <class T> ref_tensor *wrap(Tensor<T> *t) { return new ref_tensor{code<T>(), t}; }
+
+// The handle's tensor, which must hold T.
+template <class T> Tensor<T> &as(const ref_tensor *h) {
+  if (h->dtype != code<T>()) throw std::invalid_argument("tensors of different element types");
+  return *static_cast<Tensor<T> *>(h->t);
 }
 
-// The reference's destructor releases the buffer without freeing it
-// (block_sparse.h:259-262); the buffer is freed here.
-void ref_tensor_free(ref_tensor *h) {
-  if (!h) return;
-  Tensor *t = reinterpret_cast<Tensor *>(h);
-  std::free(DataAccess::release(*t));
+// ---- per-type bodies of the entry points ----
+
+template <class T> void free_t(ref_tensor *h) {
+  Tensor<T> *t = &as<T>(h);
+  std::free(DataAccess<T>::release(*t));
   delete t;
 }
 
-// contract(tensor, contracting_indices) (block_sparse.h:414-584);
-// legs is the n x 2 contracting-index matrix, column-major (column 0 = this
-// tensor's legs).
-int32_t ref_contract(const ref_tensor *a, const ref_tensor *b, int32_t n, const uint64_t *legs,
-                     ref_tensor **out) {
-  return guarded([&] {
-    const Tensor &A = *reinterpret_cast<const Tensor *>(a);
-    const Tensor &B = *reinterpret_cast<const Tensor *>(b);
-    Tensor *c = new Tensor(A.contract(B, to_umat(legs, n, 2)));
-    *out = reinterpret_cast<ref_tensor *>(c);
-  });
+template <class T> void contract_t(const ref_tensor *a, const ref_tensor *b, int32_t n,
+                                   const uint64_t *legs, ref_tensor **out) {
+  *out = wrap(new Tensor<T>(as<T>(a).contract(as<T>(b), to_umat(legs, n, 2))));
 }
 
-// hard_transpose(permutation) (block_sparse.h:607-651)
-int32_t ref_hard_transpose(const ref_tensor *a, const uint64_t *perm, ref_tensor **out) {
-  return guarded([&] {
-    const Tensor &A = *reinterpret_cast<const Tensor *>(a);
-    Tensor *c = new Tensor(A.hard_transpose(to_uvec(perm, A.rank)));
-    *out = reinterpret_cast<ref_tensor *>(c);
-  });
+template <class T> void transpose_t(const ref_tensor *a, const uint64_t *perm, ref_tensor **out) {
+  const Tensor<T> &A = as<T>(a);
+  *out = wrap(new Tensor<T>(A.hard_transpose(to_uvec(perm, A.rank))));
 }
 
-// query(indices) (block_sparse.h:372-411)
-int32_t ref_query(const ref_tensor *a, int32_t n, const uint64_t *indices, double *value) {
-  return guarded([&] {
-    const Tensor &A = *reinterpret_cast<const Tensor *>(a);
-    *value = A.query(to_uvec(indices, n));
-  });
+template <class T> void query_t(const ref_tensor *a, int32_t n, const uint64_t *idx, double *v) {
+  *v = double(as<T>(a).query(to_uvec(idx, n)));
 }
 
-// modify(indices, number) (block_sparse.h:322-369)
-int32_t ref_modify(ref_tensor *a, int32_t n, const uint64_t *indices, double number) {
-  return guarded([&] {
-    Tensor &A = *reinterpret_cast<Tensor *>(a);
-    A.modify(to_uvec(indices, n), number);
-  });
+template <class T> void modify_t(ref_tensor *a, int32_t n, const uint64_t *idx, double number) {
+  as<T>(a).modify(to_uvec(idx, n), T(number));
 }
 
-// append_block(data, begin_point, end_point, index_table) (block_sparse.h:285-317)
-int32_t ref_append_block(ref_tensor *a, int32_t rank, const double *data, const uint64_t *begin,
-                         const uint64_t *end, const uint64_t *index_table) {
-  return guarded([&] {
-    Tensor &A = *reinterpret_cast<Tensor *>(a);
-    A.append_block(data, to_uvec(begin, rank), to_uvec(end, rank), to_uvec(index_table, rank));
-  });
+template <class T> void append_t(ref_tensor *a, int32_t rank, const void *data,
+                                 const uint64_t *begin, const uint64_t *end,
+                                 const uint64_t *table) {
+  as<T>(a).append_block(static_cast<const T *>(data), to_uvec(begin, rank), to_uvec(end, rank),
+                        to_uvec(table, rank));
 }
 
-// rank, block count and element count of a tensor
-void ref_tensor_info(const ref_tensor *a, int32_t *rank, int64_t *n_blocks, int64_t *n_elem) {
-  const Tensor &A = *reinterpret_cast<const Tensor *>(a);
+template <class T> void info_t(const ref_tensor *a, int32_t *rank, int64_t *n_blocks,
+                               int64_t *n_elem) {
+  const Tensor<T> &A = as<T>(a);
   *rank = int32_t(A.rank);
   *n_blocks = int64_t(A.begin_points.n_cols);
   *n_elem = A.rank ? int64_t(arma::sum(A.block_n_elem)) : 1;
 }
 
-// The public metadata members and the values, as the tensor holds them:
-// begin/end/index tables rank x n_blocks column-major, offsets per block.
-// A null destination is skipped.
-void ref_tensor_read(const ref_tensor *a, uint64_t *dimension, uint64_t *begin, uint64_t *end,
-                     uint64_t *index_tables, uint64_t *offsets, double *data) {
-  const Tensor &A = *reinterpret_cast<const Tensor *>(a);
+template <class T> void read_t(const ref_tensor *a, uint64_t *dimension, uint64_t *begin,
+                               uint64_t *end, uint64_t *index_tables, uint64_t *offsets,
+                               void *data) {
+  const Tensor<T> &A = as<T>(a);
   if (dimension)
     for (arma::uword i = 0; i < A.dimension.n_elem; i++) dimension[i] = A.dimension[i];
   if (begin)
@@ -174,9 +144,105 @@ void ref_tensor_read(const ref_tensor *a, uint64_t *dimension, uint64_t *begin, 
     for (arma::uword i = 0; i < A.block_offsets.n_elem; i++) offsets[i] = A.block_offsets[i];
   if (data) {
     const arma::uword n = A.rank ? arma::sum(A.block_n_elem) : 1;
-    const double *p = DataAccess::get(A);
-    for (arma::uword i = 0; i < n; i++) data[i] = p[i];
+    const T *p = DataAccess<T>::get(A);
+    T *o = static_cast<T *>(data);
+    for (arma::uword i = 0; i < n; i++) o[i] = p[i];
   }
+}
+
+}  // namespace
+
+// Runs BODY<double> or BODY<float> after the element type of handle H.
+#define REF_DISPATCH(H, BODY, ...)     \
+  do {                                 \
+    if ((H)->dtype == REF_F64)         \
+      BODY<double>(__VA_ARGS__);       \
+    else                               \
+      BODY<float>(__VA_ARGS__);        \
+  } while (0)
+
+extern "C" {
+
+const char *ref_last_error(void) { return last_error.c_str(); }
+
+// BlockSparseTensor(const T*, begin_points, end_points, total_dimension)
+// (block_sparse.h:155-202).  The tensor copies the values.
+int32_t ref_tensor_new(int32_t dtype, int32_t rank, const uint64_t *dimension, int64_t n_blocks,
+                       const uint64_t *begin, const uint64_t *end, const void *data,
+                       ref_tensor **out) {
+  return guarded([&] {
+    const arma::umat b = to_umat(begin, rank, n_blocks), e = to_umat(end, rank, n_blocks);
+    const arma::uvec d = to_uvec(dimension, rank);
+    if (dtype == REF_F64)
+      *out = wrap(new Tensor<double>(static_cast<const double *>(data), b, e, d));
+    else
+      *out = wrap(new Tensor<float>(static_cast<const float *>(data), b, e, d));
+  });
+}
+
+// BlockSparseTensor(dimension) (block_sparse.h:147-153): no blocks, one
+// zeroed element (a rank-0 tensor's value).
+int32_t ref_tensor_new_empty(int32_t dtype, int32_t rank, const uint64_t *dimension,
+                             ref_tensor **out) {
+  return guarded([&] {
+    const arma::uvec d = to_uvec(dimension, rank);
+    if (dtype == REF_F64)
+      *out = wrap(new Tensor<double>(d));
+    else
+      *out = wrap(new Tensor<float>(d));
+  });
+}
+
+// The reference's destructor releases the buffer without freeing it
+// (block_sparse.h:259-262); the buffer is freed here.
+void ref_tensor_free(ref_tensor *h) {
+  if (!h) return;
+  REF_DISPATCH(h, free_t, h);
+  delete h;
+}
+
+// contract(tensor, contracting_indices) (block_sparse.h:414-584); legs is the
+// n x 2 contracting-index matrix, column-major (column 0 = this tensor's
+// legs).  Both tensors hold the same element type.
+int32_t ref_contract(const ref_tensor *a, const ref_tensor *b, int32_t n, const uint64_t *legs,
+                     ref_tensor **out) {
+  return guarded([&] { REF_DISPATCH(a, contract_t, a, b, n, legs, out); });
+}
+
+// hard_transpose(permutation) (block_sparse.h:607-651)
+int32_t ref_hard_transpose(const ref_tensor *a, const uint64_t *perm, ref_tensor **out) {
+  return guarded([&] { REF_DISPATCH(a, transpose_t, a, perm, out); });
+}
+
+// query(indices) (block_sparse.h:372-411)
+int32_t ref_query(const ref_tensor *a, int32_t n, const uint64_t *indices, double *value) {
+  return guarded([&] { REF_DISPATCH(a, query_t, a, n, indices, value); });
+}
+
+// modify(indices, number) (block_sparse.h:322-369)
+int32_t ref_modify(ref_tensor *a, int32_t n, const uint64_t *indices, double number) {
+  return guarded([&] { REF_DISPATCH(a, modify_t, a, n, indices, number); });
+}
+
+// append_block(data, begin_point, end_point, index_table) (block_sparse.h:285-317)
+int32_t ref_append_block(ref_tensor *a, int32_t rank, const void *data, const uint64_t *begin,
+                         const uint64_t *end, const uint64_t *index_table) {
+  return guarded([&] { REF_DISPATCH(a, append_t, a, rank, data, begin, end, index_table); });
+}
+
+// element type, rank, block count and element count of a tensor
+void ref_tensor_info(const ref_tensor *a, int32_t *dtype, int32_t *rank, int64_t *n_blocks,
+                     int64_t *n_elem) {
+  *dtype = a->dtype;
+  REF_DISPATCH(a, info_t, a, rank, n_blocks, n_elem);
+}
+
+// The public metadata members and the values, as the tensor holds them:
+// begin/end/index tables rank x n_blocks column-major, offsets per block,
+// values in the tensor's element type.  A null destination is skipped.
+void ref_tensor_read(const ref_tensor *a, uint64_t *dimension, uint64_t *begin, uint64_t *end,
+                     uint64_t *index_tables, uint64_t *offsets, void *data) {
+  REF_DISPATCH(a, read_t, a, dimension, begin, end, index_tables, offsets, data);
 }
 
 // block_in_range(contracting_indices, A begin, A end, B begins, B ends)
@@ -198,8 +264,8 @@ int64_t ref_block_in_range(int32_t n, const uint64_t *legs, int32_t rank_a,
   return st ? -1 : count;
 }
 
-// Register a Fortran-convention dgemm for the matrix product (the reference
-// reaches BLAS through Armadillo); null restores the loop.
+// Register a Fortran-convention dgemm for the double matrix product (the
+// reference reaches BLAS through Armadillo); null restores the loop.
 void ref_set_dgemm(void *fn) { arma::set_dgemm(reinterpret_cast<arma::dgemm_fn>(fn)); }
 
 // Seconds spent in matrix products since the last reset.

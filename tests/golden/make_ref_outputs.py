@@ -16,7 +16,8 @@ its message, and where the as-is strides would read past a tensor's values
 (the oracle's mode 2 detects it) the as-is build is not run and the case is
 marked "undefined".  Transposition, query and modify cases store their full
 results (for modify: the reads in order and the tensor afterwards).  Keys
-are "<case>__<variant>__<field>"; "<case>__input" is the sha256 of the inputs.
+are "<case>__<variant>__<field>" (variant "f32": the stride-fixed build's float
+instantiation); "<case>__input" is the sha256 of the inputs.
 """
 from __future__ import annotations
 
@@ -71,6 +72,16 @@ def main() -> None:
                 z[key + "values"] = data
             else:
                 z[key + "digest"] = rc.value_digest(offsets, rc.block_sizes(begin, end), data)
+    for name in rc.FLOAT_CASES:
+        A, B, pairs = rc.CONTRACTIONS[name]()
+        begin, end, offsets, data = ref.contract(A, B, pairs, variant="fixed", dtype=np.float32)
+        key = "%s__f32__" % name
+        z[key + "begin"], z[key + "end"], z[key + "offsets"] = begin, end, offsets
+        if data.size <= FULL_LIMIT:
+            z[key + "values"] = data
+        else:
+            z[key + "digest"] = rc.value_digest(offsets, rc.block_sizes(begin, end),
+                                                data.astype(np.float64))
     for tname, T in rc.transpose_cases().items():
         z[tname + "__input"] = np.array(rc.input_digest(T))
         for k, perm in enumerate(rc.TRANSPOSE_PERMS):

@@ -26,6 +26,8 @@ Cases:
 * ``transpose_r4_rowmajor``: the same permutations of a ragged rank-4 tensor
   whose odd blocks are stored row-major (no extent-1 legs: see below);
 * ``modify_r3``: element writes and reads on overlapping blocks;
+* ``FLOAT_CASES``: three of the contractions again through the reference's
+  ``BlockSparseTensor<float>`` (inputs rounded to float32);
 * ``query_r3``: element reads of an overlapping rank-3 tensor (overlaps add).
 """
 from __future__ import annotations
@@ -96,6 +98,9 @@ CONTRACTIONS = {
                np.random.default_rng(19).standard_normal(6 + 4 + 4)),
         np.array([[1, 0]], np.int64)),
 }
+
+# contractions also stored from the reference's float instantiation
+FLOAT_CASES = ("u1_85", "ragged_r3_k2_unsorted", "custom_tables_r3_k1")
 
 TRANSPOSE_PERMS = ([3, 1, 0, 2], [1, 0, 2, 3], [0, 1, 2, 3], [2, 3, 1, 0])
 

@@ -34,8 +34,9 @@ def fx():
     return rc.load()
 
 
-def to_gpu(tq, T):
-    return tq.BlockSparseTensor(T.dimension, T.data, T.begin.T, T.end.T, T.strides.T)
+def to_gpu(tq, T, dtype=np.float64):
+    return tq.BlockSparseTensor(T.dimension, T.data.astype(dtype), T.begin.T, T.end.T,
+                                T.strides.T, dtype=dtype)
 
 
 def check(C, fx, key, tol):
@@ -64,6 +65,26 @@ def test_native_fp64_matches_reference(tq, fx, name):
     assert rc.input_digest(A, B) == str(fx[name + "__input"])
     C = to_gpu(tq, A).contract(to_gpu(tq, B), pairs)
     check(C, fx, name + "__fixed__", TOL64)
+
+
+@pytest.mark.parametrize("name", rc.FLOAT_CASES)
+def test_native_fp32_matches_reference_float(tq, fx, name):
+    """Float tensors against the reference's float instantiation on the same
+    inputs rounded to float32: block lists bit-exact, values within 1e-5 of
+    max|C| (both accumulate in float, in different orders)."""
+    A, B, pairs = rc.CONTRACTIONS[name]()
+    C = to_gpu(tq, A, np.float32).contract(to_gpu(tq, B, np.float32), pairs)
+    key = name + "__f32__"
+    dim, b, e, t, o = C.metadata()
+    assert np.array_equal(b.T, fx[key + "begin"]) and np.array_equal(e.T, fx[key + "end"])
+    assert np.array_equal(o, fx[key + "offsets"])
+    data = C.data().astype(np.float64)
+    sizes = rc.block_sizes(b.T, e.T)
+    if key + "values" in fx:
+        want = fx[key + "values"].astype(np.float64)
+        assert np.max(np.abs(data - want)) <= 1e-5 * np.max(np.abs(want))
+    else:
+        assert rc.digest_close(rc.value_digest(o, sizes, data), fx[key + "digest"], sizes, 1e-5)
 
 
 @pytest.mark.parametrize("name", ["u1_85", "u1_85_swapped"])

@@ -83,6 +83,26 @@ def test_oracle_matches_reference_outputs(fx, name):
         compare_contraction(orc.contract(A, B, pairs, mode=mode), fx, key)
 
 
+@pytest.mark.parametrize("name", rc.FLOAT_CASES)
+def test_reference_float_outputs_agree_with_oracle(fx, name):
+    """The reference's float instantiation on the same inputs rounded to
+    float32: the block list is the double one, values within 1e-5 of max|C|
+    of the oracle's float64 result on the rounded inputs."""
+    A, B, pairs = rc.CONTRACTIONS[name]()
+    r = lambda T: orc.HostBS(T.dimension, T.begin, T.end, T.data.astype(np.float32),
+                             strides=T.strides, offsets=T.offsets)
+    ob, oe, off, want = orc.contract(r(A), r(B), pairs, mode=0)
+    key = "%s__f32__" % name
+    assert np.array_equal(ob, fx[key + "begin"]) and np.array_equal(oe, fx[key + "end"])
+    assert np.array_equal(off, fx[key + "offsets"])
+    sizes = rc.block_sizes(ob, oe)
+    if key + "values" in fx:
+        got = fx[key + "values"].astype(np.float64)
+        assert np.max(np.abs(got - want)) <= 1e-5 * np.max(np.abs(want))
+    else:
+        assert rc.digest_close(rc.value_digest(off, sizes, want), fx[key + "digest"], sizes, 1e-5)
+
+
 def test_fixture_covers_both_builds(fx):
     """The stored cases include the as-is build's wrong values (uneven
     blocks), its bounds error (more partners than A blocks) and a scalar."""
