@@ -105,6 +105,19 @@ tq_status tq_bs_create(tq_dtype dtype, int32_t rank, const int64_t *dimension,
                        const void *data, tq_memkind kind, tq_stream stream,
                        tq_bs **out);
 
+/* Adopts a device buffer the caller allocated with cudaMalloc: the reference's
+ * raw move-in constructor BlockSparseTensor(T* data, rank, dimension,
+ * blocks_dimension, begin_points, end_points, block_n_elem, block_offsets,
+ * index_tables) (block_sparse.cuh:283-304).  The tensor owns device_data from
+ * then on and frees it with cudaFree (as the reference's destructor does,
+ * :361-364); no copy is made.  block_offsets may be NULL; if given it must be
+ * the exclusive scan of the block sizes (TQ_ERR_UNSUPPORTED otherwise).  On
+ * any error the buffer stays the caller's. */
+tq_status tq_bs_adopt(tq_dtype dtype, int32_t rank, const int64_t *dimension, int64_t n_blocks,
+                      const int64_t *begin_points, const int64_t *end_points,
+                      const int64_t *index_tables, const int64_t *block_offsets,
+                      void *device_data, tq_bs **out);
+
 /* The same block list with every element zero (the reference's
  * DenseTensor(dimension) and SparseTensor(dimension) constructors,
  * src/gpu/dense.cuh:68-84, src/gpu/sparse.cuh:95-103, start from zeros). */

@@ -109,6 +109,36 @@ class BlockSparseTensor {
     create(source_data, begin, end, total_dimension, &tables, kind);
   }
 
+  // The raw move-in constructor (block_sparse.cuh:283-304): takes ownership of
+  // `data`, a device buffer the caller allocated with cudaMalloc, without a
+  // copy; the tensor frees it with cudaFree.  The redundant metadata
+  // (blocks_dimension, block_n_elem, block_offsets) must agree with the boxes
+  // (Error otherwise, and the buffer stays the caller's).
+  BlockSparseTensor(T *data, arma::uword rank, arma::uvec &&dimension,
+                    arma::umat &&blocks_dimension, arma::umat &&begin_points,
+                    arma::umat &&end_points, arma::uvec &&block_n_elem,
+                    arma::uvec &&block_offsets, arma::umat &&index_tables) {
+    if (dimension.n_elem != rank) throw Error("Rank does not match");
+    const int64_t nb = rank ? (int64_t)begin_points.n_cols : 0;
+    for (int64_t k = 0; k < nb; k++) {
+      arma::uword cnt = 1;
+      for (arma::uword l = 0; l < rank; l++) {
+        const arma::uword d = end_points(l, k) - begin_points(l, k) + 1;
+        if (blocks_dimension(l, k) != d)
+          throw Error("blocks_dimension does not match the begin and end points");
+        cnt *= d;
+      }
+      if (block_n_elem(k) != cnt) throw Error("block_n_elem does not match the block boxes");
+    }
+    const auto d = detail::flat(dimension), b = detail::flat(begin_points),
+               e = detail::flat(end_points), t = detail::flat(index_tables),
+               off = detail::flat(block_offsets);
+    detail::check(tq_bs_adopt(detail::dtype<T>(), (int32_t)rank, d.data(), nb, b.data(), e.data(),
+                              index_tables.n_elem ? t.data() : nullptr,
+                              block_offsets.n_elem ? off.data() : nullptr, data, &h_));
+    refresh();
+  }
+
   BlockSparseTensor(const BlockSparseTensor &o) {
     detail::check(tq_bs_clone(o.h_, nullptr, &h_));
     refresh();

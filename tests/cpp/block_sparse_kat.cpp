@@ -191,11 +191,47 @@ static void factorisations() {
   EXPECT(std::fabs(s2 - norm2) <= 1e-12 * norm2);
 }
 
+// The raw move-in constructor (block_sparse.cuh:283-304): a cudaMalloc'd
+// buffer holding two column-major blocks of a 4 x 3 matrix, rows 0-1 x
+// columns 0-1 (values 1..4) and rows 1-3 x columns 1-2 (values 5..10), is
+// adopted without a copy and read back (the blocks overlap at (1, 1): 4 + 5);
+// append_block then replaces the adopted buffer (the tensor frees it) and the
+// tensor's destructor frees the rest.  Metadata that disagrees with the boxes
+// throws Error before anything is adopted.
+static void move_in() {
+  using torque::gpu::BlockSparseTensor;
+  const std::vector<double> h = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10};
+  double *d = nullptr;
+  EXPECT(cudaMalloc(reinterpret_cast<void **>(&d), h.size() * sizeof(double)) == cudaSuccess);
+  EXPECT(cudaMemcpy(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice) ==
+         cudaSuccess);
+  bool threw = false;
+  try {  // blocks_dimension says block 1 has one column; its box has two
+    BlockSparseTensor<double> bad(d, 2, arma::uvec{4, 3}, arma::umat{{2, 3}, {2, 1}},
+                                  arma::umat{{0, 1}, {0, 1}}, arma::umat{{1, 3}, {1, 2}},
+                                  arma::uvec{4, 6}, arma::uvec{0, 4}, arma::umat{{1, 1}, {2, 3}});
+  } catch (const Error &) {
+    threw = true;
+  }
+  EXPECT(threw);
+  BlockSparseTensor<double> t(d, 2, arma::uvec{4, 3}, arma::umat{{2, 3}, {2, 2}},
+                              arma::umat{{0, 1}, {0, 1}}, arma::umat{{1, 3}, {1, 2}},
+                              arma::uvec{4, 6}, arma::uvec{0, 4}, arma::umat{{1, 1}, {2, 3}});
+  EXPECT(t.begin_points.n_cols == 2 && t.block_offsets(1) == 4 && t.index_tables(1, 1) == 3);
+  EXPECT(t.query({0, 0}) == 1 && t.query({1, 0}) == 2 && t.query({0, 1}) == 3);
+  EXPECT(t.query({1, 1}) == 4 + 5);
+  EXPECT(t.query({1, 2}) == 8 && t.query({3, 2}) == 10 && t.query({0, 2}) == 0);
+  const std::vector<double> extra = {11};
+  t.append_block(extra.data(), arma::uvec{3, 0}, arma::uvec{3, 0}, arma::uvec{1, 1});
+  EXPECT(t.query({3, 0}) == 11 && t.query({3, 2}) == 10 && t.query({1, 1}) == 9);
+}
+
 int main() {
   run_cases<float>();
   run_cases<double>();
   run_cases<__half>();
   factorisations();
+  move_in();
   std::printf("%s (%d failed checks)\n", g_failed ? "FAIL" : "OK", g_failed);
   return g_failed;
 }

@@ -30,9 +30,11 @@ def build_kat(tmp_path, src=SRC):
     lib = tq_build.build()
     exe = str(tmp_path / os.path.splitext(os.path.basename(src))[0])
     libdir = os.path.dirname(lib)
+    cuda_lib = os.path.join(os.path.dirname(cuda_include()), "lib64")
+    # the CUDA runtime too: the move-in case allocates its buffer with cudaMalloc
     cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"),
            "-I" + cuda_include(), "-o", exe, src, "-L" + libdir, "-ltorque_gb300",
-           "-Wl,-rpath," + libdir]
+           "-Wl,-rpath," + libdir, "-L" + cuda_lib, "-lcudart", "-Wl,-rpath," + cuda_lib]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     return exe

@@ -43,6 +43,7 @@ SIGNATURES = {
     "tq_bs_create": (ST, [I32, I32, P64, I64, P64, P64, P64, P, I32, P, PP]),
     "tq_bs_clone": (ST, [P, P, PP]),
     "tq_bs_create_zeros": (ST, [I32, I32, P64, I64, P64, P64, P64, P, PP]),
+    "tq_bs_adopt": (ST, [I32, I32, P64, I64, P64, P64, P64, P64, P, PP]),
     "tq_bs_set_data": (ST, [P, P, I32, P]),
     "tq_bs_set_data_async": (ST, [P, P, I32, P]),
     "tq_bs_destroy": (ST, [P]),

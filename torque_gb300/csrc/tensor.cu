@@ -92,9 +92,22 @@ tq_bs *new_tensor(tq_dtype dt, int32_t rank, const int64_t *dimension) {
   return t;
 }
 
-tq_status alloc_data(tq_bs *t, int64_t n_elem, cudaStream_t s) {
-  if (t->data) dev_free(t->data, t->alloc_stream);
+// Frees a tensor's value buffer: the library pool's stream-ordered free, or
+// cudaFree for a buffer adopted from the caller (tq_bs_adopt), which waits
+// for the work queued on the device.
+static void free_data(tq_bs *t) {
+  if (t->data) {
+    if (t->adopted)
+      cudaFree(t->data);
+    else
+      dev_free(t->data, t->alloc_stream);
+  }
   t->data = nullptr;
+  t->adopted = false;
+}
+
+tq_status alloc_data(tq_bs *t, int64_t n_elem, cudaStream_t s) {
+  free_data(t);
   t->alloc_stream = s;
   int64_t cap = n_elem > 0 ? n_elem : 1;
   TQ_CHECK(dev_alloc(&t->data, (size_t)cap * dtype_size(t->dtype), s));
@@ -277,6 +290,46 @@ tq_status tq_bs_create(tq_dtype dtype, int32_t rank, const int64_t *dimension, i
   return TQ_OK;
 }
 
+tq_status tq_bs_adopt(tq_dtype dtype, int32_t rank, const int64_t *dimension, int64_t n_blocks,
+                      const int64_t *begin_points, const int64_t *end_points,
+                      const int64_t *index_tables, const int64_t *block_offsets,
+                      void *device_data, tq_bs **out) {
+  if (!out) return fail(TQ_ERR_INVALID, "out is NULL");
+  if (!device_data) return fail(TQ_ERR_INVALID, "Source data not allocated!");
+  if (n_blocks < 0) return fail(TQ_ERR_INVALID, "negative block count");
+  if (rank < 0 || rank > TQ_MAXR) return fail(TQ_ERR_UNSUPPORTED, "rank outside 0..12");
+  if (rank && !dimension) return fail(TQ_ERR_INVALID, "dimension is NULL");
+  if (dtype != TQ_F32 && dtype != TQ_F64 && dtype != TQ_F16)
+    return fail(TQ_ERR_INVALID, "unknown dtype");
+  if (rank == 0) n_blocks = 0;
+  if (n_blocks && (!begin_points || !end_points))
+    return fail(TQ_ERR_INVALID, "begin/end points are NULL");
+  TQ_CHECK(check_boxes(rank, dimension, n_blocks, begin_points, end_points));
+  tq_bs *t = new_tensor(dtype, rank, dimension);
+  int64_t added = 0;
+  append_meta(t, n_blocks, begin_points, end_points, index_tables, &added);
+  if (block_offsets)
+    for (int64_t k = 0; k < n_blocks; k++)
+      if (block_offsets[k] != t->h_offsets[k]) {
+        tq_bs_destroy(t);  // the buffer is still the caller's
+        return fail(TQ_ERR_UNSUPPORTED,
+                    "block offsets must be the exclusive scan of the block sizes");
+      }
+  t->data = device_data;
+  t->adopted = true;
+  t->n_elem = rank == 0 ? 1 : added;
+  t->capacity = t->n_elem;
+  const tq_status st = sync_device_meta(t, nullptr);
+  if (st != TQ_OK) {
+    t->data = nullptr;  // a failed adoption leaves the buffer with the caller
+    t->adopted = false;
+    tq_bs_destroy(t);
+    return st;
+  }
+  *out = t;
+  return TQ_OK;
+}
+
 tq_status tq_bs_create_zeros(tq_dtype dtype, int32_t rank, const int64_t *dimension,
                              int64_t n_blocks, const int64_t *begin_points,
                              const int64_t *end_points, const int64_t *index_tables,
@@ -361,7 +414,7 @@ tq_status tq_bs_clone(const tq_bs *src, tq_stream stream, tq_bs **out) {
 
 tq_status tq_bs_destroy(tq_bs *t) {
   if (!t) return TQ_OK;
-  if (t->data) dev_free(t->data, t->alloc_stream);
+  free_data(t);
   t->d_meta.release();
   delete t;
   return TQ_OK;
@@ -403,7 +456,7 @@ tq_status tq_bs_append_blocks(tq_bs *t, int64_t n, const int64_t *b, const int64
         return cuda_fail(err, "cudaMemcpyAsync");
       }
     }
-    dev_free(t->data, t->alloc_stream);
+    free_data(t);
     t->data = nd;
     t->alloc_stream = s;
     t->capacity = cap;

@@ -134,6 +134,7 @@ struct tq_bs {
   int64_t n_elem = 0;      // elements in use
   int64_t capacity = 0;    // elements allocated
   cudaStream_t alloc_stream = nullptr;
+  bool adopted = false;    // data is a caller's cudaMalloc buffer (tq_bs_adopt): cudaFree
 
   tq::DevBS view() const {
     tq::DevBS v;
