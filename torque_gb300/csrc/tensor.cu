@@ -92,15 +92,17 @@ tq_bs *new_tensor(tq_dtype dt, int32_t rank, const int64_t *dimension) {
   return t;
 }
 
-// Frees a tensor's value buffer: the library pool's stream-ordered free, or
-// cudaFree for a buffer adopted from the caller (tq_bs_adopt), which waits
-// for the work queued on the device.
+// Frees a tensor's value buffer: the library pool's stream-ordered free, or,
+// for a buffer adopted from the caller (tq_bs_adopt), cudaFree after the work
+// queued on the device (a copy out of it on any stream) has finished.
 static void free_data(tq_bs *t) {
   if (t->data) {
-    if (t->adopted)
+    if (t->adopted) {
+      cudaDeviceSynchronize();
       cudaFree(t->data);
-    else
+    } else {
       dev_free(t->data, t->alloc_stream);
+    }
   }
   t->data = nullptr;
   t->adopted = false;
