@@ -241,8 +241,9 @@ def sampled_error(c, a_dev, b_dev, C, n_largest=2, n_random=4, seed=5):
     blocks are [a,b | c,d] and B's [c,d | e,f], column-major, so each is that
     matrix as stored).  Reports, over the sampled blocks: the normwise error
     max|C - ref| / max|ref| per block, and the elementwise error against the
-    product of magnitudes, max |C - ref| / (|A||B|) per element (the form the
-    slicing error bound takes)."""
+    product of magnitudes, max |C - ref| / (|A||B|) per element (the slicing
+    bound itself scales with each row's and column's largest element, which
+    is at least this)."""
     pa, pb = host_pairs(c)
     fl = pair_flops(c, pa, pb)
     dim, b, e, t, off = C.metadata()
