@@ -301,3 +301,45 @@ def test_live_modify_fixture_is_current(fx):
     assert np.array_equal(H.strides, fx["modify_r3__tables"])
     assert np.array_equal(H.data, fx["modify_r3__values"])
     assert H.n_blocks > M.n_blocks       # writes outside every block appended blocks
+
+
+def _ref_partners_chunk(args):
+    """Worker: the reference's block_in_range for a range of A blocks of the
+    full uneven case; returns (A block, partner) pairs in order."""
+    lo, hi = args
+    from oracle import ref as r
+    from torque_gb300 import workloads
+    c = workloads.uneven_u1(data=False)
+    out = []
+    for i in range(lo, hi):
+        found = r.block_in_range(c.pairs, c.A.begin[i], c.A.end[i], c.B.begin, c.B.end)
+        out.append(np.stack([np.full(found.size, i, np.int64), found], 1))
+    return np.concatenate(out) if out else np.zeros((0, 2), np.int64)
+
+
+@live
+def test_live_full_size_pair_list_is_the_references():
+    """The full uneven case (23,969 blocks per tensor): the reference's own
+    block matcher (block_in_range, block_sparse.cpp:6-175), run for every A
+    block against all B blocks (5.7e8 interval tests, spread over worker
+    processes), gives the oracle's 593,505-pair list in the same order; the
+    CUDA path's list equals the oracle's at this size
+    (tests/test_gpu_headline_structure.py)."""
+    import concurrent.futures
+    import multiprocessing
+    from torque_gb300 import workloads
+    c = workloads.uneven_u1(data=False)
+    z = np.zeros(1)
+    A = orc.HostBS(c.A.dimension, c.A.begin, c.A.end, z)
+    B = orc.HostBS(c.B.dimension, c.B.begin, c.B.end, z)
+    pa, pb = orc.match(A, B, c.pairs)
+    n = A.n_blocks
+    workers = max(1, min(8, os.cpu_count() or 1))
+    bounds = np.linspace(0, n, 4 * workers + 1).astype(int)
+    chunks = [(int(bounds[k]), int(bounds[k + 1])) for k in range(len(bounds) - 1)]
+    ctx = multiprocessing.get_context("spawn")
+    with concurrent.futures.ProcessPoolExecutor(workers, mp_context=ctx) as ex:
+        parts = list(ex.map(_ref_partners_chunk, chunks))
+    got = np.concatenate(parts)
+    assert got.shape[0] == 593505 == pa.size
+    assert np.array_equal(got[:, 0], pa) and np.array_equal(got[:, 1], pb)
