@@ -75,7 +75,7 @@ def lib(variant: str = "fixed"):
         L.ref_tensor_read.argtypes = [ctypes.c_void_p, U, U, U, U, U, ctypes.c_void_p]
         L.ref_block_in_range.restype = ctypes.c_int64
         L.ref_block_in_range.argtypes = [ctypes.c_int32, U, ctypes.c_int32, U, U,
-                                         ctypes.c_int32, ctypes.c_int64, U, U, U,
+                                         ctypes.c_int32, ctypes.c_int64, U, U, U, U, U,
                                          ctypes.c_int64]
         L.ref_set_dgemm.argtypes = [ctypes.c_void_p]
         L.ref_product_seconds.restype = ctypes.c_double
@@ -237,9 +237,12 @@ def query(T: HostBS, idx, variant: str = "fixed") -> float:
     return RefTensor.from_host(T, variant).query(idx)
 
 
-def block_in_range(pairs, a_begin, a_end, b_begin, b_end, variant: str = "fixed") -> np.ndarray:
+def block_in_range(pairs, a_begin, a_end, b_begin, b_end, variant: str = "fixed",
+                   boxes: bool = False):
     """Indices of the B blocks (rows of b_begin/b_end, [n_b, rank]) whose
-    contracted intervals meet the A block (a_begin/a_end, [rank])."""
+    contracted intervals meet the A block (a_begin/a_end, [rank]); with
+    boxes=True also each pair's output box as (indices, begin [count, rank_out],
+    end [count, rank_out])."""
     L = lib(variant)
     legs = _legs(pairs)
     ab = np.ascontiguousarray(a_begin, np.uint64)
@@ -247,12 +250,20 @@ def block_in_range(pairs, a_begin, a_end, b_begin, b_end, variant: str = "fixed"
     bb = np.ascontiguousarray(b_begin, np.uint64)
     be = np.ascontiguousarray(b_end, np.uint64)
     nb = bb.shape[0]
+    ro = ab.size + bb.shape[1] - 2 * (legs.size // 2)
     found = np.zeros(max(nb, 1), np.uint64)
+    nbeg = np.zeros(max(nb * max(ro, 1), 1), np.uint64) if boxes else None
+    nend = np.zeros_like(nbeg) if boxes else None
     n = L.ref_block_in_range(legs.size // 2, _u(legs), ab.size, _u(ab), _u(ae), bb.shape[1], nb,
-                             _u(bb), _u(be), _u(found), nb)
+                             _u(bb), _u(be), _u(found), _u(nbeg) if boxes else None,
+                             _u(nend) if boxes else None, nb)
     if n < 0:
         raise RefError(2, L.ref_last_error().decode())
-    return found[:n].astype(np.int64)
+    idx = found[:n].astype(np.int64)
+    if not boxes:
+        return idx
+    return (idx, nbeg[:n * ro].reshape(n, ro).astype(np.int64),
+            nend[:n * ro].reshape(n, ro).astype(np.int64))
 
 
 def use_blas(threads: int = 1, variant: str = "fixed") -> str | None:

@@ -247,19 +247,29 @@ void ref_tensor_read(const ref_tensor *a, uint64_t *dimension, uint64_t *begin, 
 
 // block_in_range(contracting_indices, A begin, A end, B begins, B ends)
 // (block_sparse.cpp:6-175): the B blocks whose contracted intervals meet the
-// A block.  Writes up to cap indices; returns how many there are (or -1 with
-// ref_last_error set).
+// A block, and each pair's output box (new_begin_points / new_end_points:
+// A's free legs then B's, rank_out x count column-major).  Writes up to cap
+// pairs (boxes skipped where the destinations are null); returns how many
+// there are (or -1 with ref_last_error set).
 int64_t ref_block_in_range(int32_t n, const uint64_t *legs, int32_t rank_a,
                            const uint64_t *a_begin, const uint64_t *a_end, int32_t rank_b,
                            int64_t n_b, const uint64_t *b_begin, const uint64_t *b_end,
-                           uint64_t *found, int64_t cap) {
+                           uint64_t *found, uint64_t *new_begin, uint64_t *new_end,
+                           int64_t cap) {
   int64_t count = -1;
   const int32_t st = guarded([&] {
     const auto info = torque::block_sparse::block_in_range(
         to_umat(legs, n, 2), to_uvec(a_begin, rank_a), to_uvec(a_end, rank_a),
         to_umat(b_begin, rank_b, n_b), to_umat(b_end, rank_b, n_b));
     count = int64_t(info.block_indices.n_elem);
-    for (int64_t i = 0; i < count && i < cap; i++) found[i] = info.block_indices[i];
+    const int64_t m = count < cap ? count : cap;
+    for (int64_t i = 0; i < m; i++) found[i] = info.block_indices[i];
+    const arma::uword ro = info.new_begin_points.n_rows;
+    if (new_begin && new_end && count)
+      for (arma::uword i = 0; i < ro * arma::uword(m); i++) {
+        new_begin[i] = info.new_begin_points[i];
+        new_end[i] = info.new_end_points[i];
+      }
   });
   return st ? -1 : count;
 }

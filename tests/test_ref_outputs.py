@@ -312,9 +312,11 @@ def _ref_partners_chunk(args):
     c = workloads.uneven_u1(data=False)
     out = []
     for i in range(lo, hi):
-        found = r.block_in_range(c.pairs, c.A.begin[i], c.A.end[i], c.B.begin, c.B.end)
-        out.append(np.stack([np.full(found.size, i, np.int64), found], 1))
-    return np.concatenate(out) if out else np.zeros((0, 2), np.int64)
+        found, nb, ne = r.block_in_range(c.pairs, c.A.begin[i], c.A.end[i], c.B.begin, c.B.end,
+                                          boxes=True)
+        out.append(np.concatenate([np.full((found.size, 1), i, np.int64), found[:, None], nb, ne],
+                                  1))
+    return np.concatenate(out) if out else np.zeros((0, 10), np.int64)
 
 
 @live
@@ -322,9 +324,9 @@ def test_live_full_size_pair_list_is_the_references():
     """The full uneven case (23,969 blocks per tensor): the reference's own
     block matcher (block_in_range, block_sparse.cpp:6-175), run for every A
     block against all B blocks (5.7e8 interval tests, spread over worker
-    processes), gives the oracle's 593,505-pair list in the same order; the
-    CUDA path's list equals the oracle's at this size
-    (tests/test_gpu_headline_structure.py)."""
+    processes), gives the oracle's 593,505-pair list in the same order, the
+    same output boxes and offsets; the CUDA path's list equals the oracle's at
+    this size (tests/test_gpu_headline_structure.py)."""
     import concurrent.futures
     import multiprocessing
     from torque_gb300 import workloads
@@ -343,3 +345,9 @@ def test_live_full_size_pair_list_is_the_references():
     got = np.concatenate(parts)
     assert got.shape[0] == 593505 == pa.size
     assert np.array_equal(got[:, 0], pa) and np.array_equal(got[:, 1], pb)
+    # each pair's output box (A's free legs then B's), and the offsets as the
+    # exclusive scan of the box sizes (nest_sum), as the oracle's block list
+    _, _, ob, oe, off = orc.contract_blocks(A, B, c.pairs)
+    assert np.array_equal(got[:, 2:6], ob) and np.array_equal(got[:, 6:10], oe)
+    sizes = np.prod(got[:, 6:10] - got[:, 2:6] + 1, axis=1)
+    assert np.array_equal(np.concatenate([[0], np.cumsum(sizes)[:-1]]), off)
