@@ -9,11 +9,13 @@ passes.  This checks the API subset that the oracle build of the reference
 
 GPU suites: they compile and link, unchanged, against the drop-in headers.
 
-test/gpu/block_sparse_test.cu and test/gpu/dense_test.cu of the reference
-include "gpu/block_sparse.cuh" / "gpu/dense.cuh"; tests/ref_suite/ maps those
-names to include/torque_gb300/block_sparse.hpp / dense.hpp (plus cuBLAS's
-declarations and the reference's CPU tensors, as the reference headers bring
-them in), Armadillo is the project's API subset (oracle/arma_api) and Catch2
+test/gpu/block_sparse_test.cu, dense_test.cu and cpu_gpu_comparison.cu of the
+reference include "gpu/block_sparse.cuh", "gpu/dense.cuh" and "gpu/sparse.cuh";
+tests/ref_suite/ maps those names to include/torque_gb300/block_sparse.hpp,
+dense.hpp and sparse.hpp (plus cuBLAS's declarations and the reference's CPU
+tensors, as the reference headers bring them in; cpu_gpu_comparison.cu checks
+the GPU classes against the reference's CPU classes, linked from its
+sources), Armadillo is the project's API subset (oracle/arma_api) and Catch2
 is the copy the reference vendors.  The programs are linked against
 libtorque_gb300.so and cuBLAS (for the handle the tests create) but not run:
 the reference's sources exist only where it is checked out, which has no GPU;
@@ -51,7 +53,7 @@ def catch_main(tmp_path_factory):
     return obj
 
 
-@pytest.mark.parametrize("name", ["block_sparse_test", "dense_test"])
+@pytest.mark.parametrize("name", ["block_sparse_test", "dense_test", "cpu_gpu_comparison"])
 def test_reference_gpu_test_builds_against_dropin(tmp_path, catch_main, name):
     from torque_gb300 import build as tq_build
     lib = tq_build.build()
@@ -62,9 +64,11 @@ def test_reference_gpu_test_builds_against_dropin(tmp_path, catch_main, name):
            "-I" + SUITE, "-I" + os.path.join(ROOT, "include"),
            "-I" + os.path.join(ROOT, "oracle", "arma_api"), "-I" + os.path.join(REF, "src"),
            "-I" + os.path.join(REF, "external", "catch2"), "-I" + os.path.join(cuda, "include"),
-           os.path.join(REF, "test", "gpu", name + ".cu"), "-x", "none", catch_main,
-           "-L" + libdir, "-ltorque_gb300", "-Wl,-rpath," + libdir,
-           "-L" + os.path.join(cuda, "lib64"), "-lcublas", "-lcudart", "-o", exe]
+           os.path.join(REF, "test", "gpu", name + ".cu"), "-x", "none"] + \
+        [os.path.join(REF, "src", "tensor", f) for f in ("block_sparse.cpp", "sparse.cpp",
+                                                         "dense.cpp")] + \
+        ["-w", catch_main, "-L" + libdir, "-ltorque_gb300", "-Wl,-rpath," + libdir,
+         "-L" + os.path.join(cuda, "lib64"), "-lcublas", "-lcudart", "-o", exe]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
     assert os.path.getsize(exe) > 0
