@@ -9,8 +9,8 @@ passes.  This checks the API subset that the oracle build of the reference
 
 GPU suites: they compile and link, unchanged, against the drop-in headers.
 
-test/gpu/block_sparse_test.cu, dense_test.cu and cpu_gpu_comparison.cu of the
-reference include "gpu/block_sparse.cuh", "gpu/dense.cuh" and "gpu/sparse.cuh";
+test/gpu/block_sparse_test.cu, dense_test.cu, cpu_gpu_comparison.cu,
+peps_test.cu, dense_peps_test.cu and the two benchmarks of the reference include "gpu/block_sparse.cuh", "gpu/dense.cuh" and "gpu/sparse.cuh";
 tests/ref_suite/ maps those names to include/torque_gb300/block_sparse.hpp,
 dense.hpp and sparse.hpp (plus cuBLAS's declarations and the reference's CPU
 tensors, as the reference headers bring them in; cpu_gpu_comparison.cu checks
@@ -53,7 +53,9 @@ def catch_main(tmp_path_factory):
     return obj
 
 
-@pytest.mark.parametrize("name", ["block_sparse_test", "dense_test", "cpu_gpu_comparison"])
+@pytest.mark.parametrize("name", ["block_sparse_test", "dense_test", "cpu_gpu_comparison",
+                                  "peps_test", "dense_peps_test", "block_sparse_benchmark",
+                                  "large_tensor_benchmark"])
 def test_reference_gpu_test_builds_against_dropin(tmp_path, catch_main, name):
     from torque_gb300 import build as tq_build
     lib = tq_build.build()
