@@ -191,6 +191,16 @@ int main() {
   CHECK(equal(uvec{0, 2, 0} == 0, {1, 0, 1}));
   CHECK(equal(arma::find(uvec{0, 2, 0} != 0), {1}));
 
+  // arithmetic with a scalar on the right; randu in [0, 1)
+  CHECK(equal(uvec{4, 5} - 1, {3, 4}) && equal(uvec{4, 5} + 2, {6, 7}));
+  CHECK(equal(uvec{4, 6} * 2, {8, 12}) && equal(uvec{4, 6} / 2, {2, 3}));
+  arma::vec r = arma::randu<arma::vec>(100);
+  CHECK(r.n_rows == 100 && r.n_cols == 1);
+  bool in_range = true;
+  for (uword i = 0; i < r.n_elem; i++) in_range = in_range && r[i] >= 0.0 && r[i] < 1.0;
+  const double u1 = arma::randu();
+  CHECK(in_range && u1 >= 0.0 && u1 < 1.0 && r[0] != r[1]);
+
   // copies of large (heap) and small (in-object) vectors are independent
   uvec big(20);
   big[19] = 5;
